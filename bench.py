@@ -1,0 +1,383 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 Givens hot path: the bulk application of k x (n-1) rotations to an
+m x n matrix (bulk_wave_order_2x2_rmul!, src/wave.jl:36-162; benchmark/benchmark.jl:4-30),
+on the microbenchmark workload Q 16384 x 16384 column-major FP64 ~ U[-1,1), k = 64 layers of
+n-1 rotations (c,s) = (cos t, sin t), t ~ U[0, 2 pi).  Reported metric: Givens GFLOP/s with
+6 flops per rotation per row (benchmark/benchmark.jl:10-11).
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference] [--dtype f64|f32]
+
+One JSON line on rank 0.  `value` is device-timed with Q resident in HBM (Q is 2.1 GB, far
+larger than the 129 MB L2, so no flush is needed between steps); `e2e` goes through the C ABI
+entry point with pinned host buffers, copies included.  Under torchrun every rank runs its own
+replica on its own GPU (the path does not shard; the reference's row slabs would need only a
+broadcast of (c,s)), and `value` sums the replicas' work over the slowest rank's time.
+`--impl reference` times the CPU restatement of the reference's wave kernel
+(oracle/symeig_oracle.c, row-slab threaded like src/wave.jl:36-60) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+WORKLOAD = "bulk Givens apply: Q 16384x16384 column-major, k=64 layers of 16383 rotations (cos t, sin t)"
+METRIC = "Givens GFLOP/s (6 flops per rotation per row), bulk apply 16384x16384 k=64"
+TRAFFIC_FILE = ROOT / "profiles" / "wave_apply_f64_16384_k64.md"
+
+
+def parse_args():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--dtype", choices=["f64", "f32"], default="f64")
+    p.add_argument("--m", type=int, default=16384)
+    p.add_argument("--n", type=int, default=16384)
+    p.add_argument("--k", type=int, default=64)
+    p.add_argument("--no-extras", action="store_true", help="skip the FP32 and n=2000 side measurements")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def flops_per_step(m, n, k):
+    return 6.0 * k * (n - 1) * m
+
+
+def make_inputs(m, n, k, dtype, seed, device):
+    import torch
+    g = torch.Generator(device="cpu").manual_seed(seed)
+    tdt = torch.float64 if dtype == "f64" else torch.float32
+    # column-major Q: a row-major (n, m) tensor viewed transposed
+    Qt = (torch.rand(n, m, generator=g, dtype=torch.float64) * 2 - 1).to(tdt)
+    th = torch.rand(k, n - 1, generator=g, dtype=torch.float64) * (2 * np.pi)
+    cs = torch.stack([torch.cos(th), torch.sin(th)], -1).to(tdt).contiguous()  # Julia layout
+    if device is not None:
+        return Qt.to(device).T, cs.to(device)
+    return Qt.T, cs
+
+
+# ---- clocks -------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index: int):
+        self.proc = None
+        self.device_index = device_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax = float(f[1])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- CPU side (the oracle's port of the reference's wave kernel) ---------------------------
+def cpu_wave_gflops(m, n, k, dtype, threads, target_s=8.0, max_rows=None):
+    """Time the reference's wave-order kernel (C port, row slabs on `threads` threads) on a
+    bounded row sample of the workload; GFLOP/s scales with rows, so the sample is
+    representative.  Returns (gflops, rows, seconds)."""
+    from oracle import oracle as orc
+    orc.build()
+    rng = np.random.default_rng(1)
+    npdt = np.float64 if dtype == "f64" else np.float32
+    th = rng.random((n - 1, k)) * 2 * np.pi
+    cs = np.empty((n - 1, k, 2), dtype=npdt)
+    cs[..., 0] = np.cos(th)
+    cs[..., 1] = np.sin(th)
+    kk = k if k % 2 == 0 else k - 1          # the reference kernel needs even k and odd n-1
+    nn = n if (n - 1) % 2 == 1 else n - 1
+    cs = np.asfortranarray(cs[: nn - 1, :kk])
+    rows = min(m, max(threads * 64, 256))
+    while True:
+        Q = np.asfortranarray(rng.random((rows, nn)).astype(npdt) * 2 - 1)
+        t0 = time.perf_counter()
+        orc.apply_wave(Q, cs, nthreads=threads)
+        dt = time.perf_counter() - t0
+        cap = max_rows or m
+        if dt >= target_s * 0.5 or rows >= cap:
+            return flops_per_step(rows, nn, kk) / dt / 1e9, rows, dt, (rows, nn, kk)
+        rows = int(min(cap, rows * max(2.0, min(16.0, target_s / max(dt, 1e-3)))))
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    vals = []
+    sample = None
+    for i in range(args.warmup + args.steps):
+        gf, rows, dt, shape = cpu_wave_gflops(args.m, args.n, args.k, args.dtype, threads, target_s=4.0)
+        sample = shape
+        if i >= args.warmup:
+            vals.append((gf, dt))
+    v = statistics.median([x[0] for x in vals])
+    ms = statistics.median([x[1] for x in vals]) * 1e3
+    desc = (f"C port of the reference's wave kernel (oracle/symeig_oracle.c), {threads} threads, "
+            f"row sample {sample[0]} of {args.m} rows x {sample[1]} cols, k={sample[2]}")
+    line = {
+        "metric": METRIC, "value": round(v, 3), "unit": "GFLOP/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.dtype, "data": "synthetic (seeded U[-1,1) Q, (cos t, sin t) rotations)",
+        "config": {"workload": WORKLOAD, "m": args.m, "n": args.n, "k": args.k, "parallelism": "cpu threads",
+                   "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": round(v, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+                         "sample": desc},
+        "e2e": {"value": round(v, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def read_traffic():
+    """DRAM bytes per launch of the wave kernel from the committed ncu summary, if present."""
+    try:
+        for ln in TRAFFIC_FILE.read_text().splitlines():
+            if ln.startswith("traffic_bytes_per_launch:"):
+                return float(ln.split(":", 1)[1].strip())
+    except Exception:
+        pass
+    return None
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    import __graft_entry__ as ge
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    pkg = ge.load_package()
+    lib = pkg.load_library()
+    h = pkg.Handle(local)
+    stream = torch.cuda.Stream(dev)
+    h.set_stream(stream.cuda_stream)
+    h.set_kernel_timing(True)
+
+    m, n, k = args.m, args.n, args.k
+    import ctypes
+    fn = getattr(lib, f"symeig_apply_givens_{args.dtype}_dev")
+    Q, cs = make_inputs(m, n, k, args.dtype, seed=1234 + rank, device=dev)
+    ld = Q.stride(1)
+
+    def step():
+        rc = fn(h.ptr, ctypes.c_void_p(Q.data_ptr()), ld, m, n, ctypes.c_void_p(cs.data_ptr()), k)
+        if rc != 0:
+            raise RuntimeError(f"symeig_apply_givens_{args.dtype}_dev -> {rc}")
+
+    torch.cuda.synchronize()
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    kernel_ms, launches = [], 0
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+            st = h.stats()   # waits for the step's last wave kernel; per-kernel device time
+            kernel_ms.append(st["wave_kernel_ms"] / max(st["wave_launches"], 1))
+            launches += 2 * st["wave_launches"]   # table build + wave kernel per pass
+        e1.record(stream)
+        torch.cuda.synchronize()
+    clocks = clk.summary()
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    ms_per_step = ms / args.steps
+    fl = flops_per_step(m, n, k)
+    value = fl * world / (ms_per_step * 1e-3) / 1e9
+
+    # roofline of the dominant kernel: the FP64 (FP32) FMA pipe
+    peak = pkg._lib.measure_fma_peak(local, fp64=(args.dtype == "f64"))
+    per_launch_ms = statistics.median(kernel_ms)
+    passes = max(1, -(-k // 64))
+    achieved = fl / passes / (per_launch_ms * 1e-3) / 1e12
+    algo_bytes = (2.0 * m * n + 2.0 * (n - 1) * k) * (8 if args.dtype == "f64" else 4)
+
+    # e2e through the host-pointer C ABI entry point, pinned buffers, copies in the timed region
+    hq = torch.empty((n, m), dtype=Q.dtype, pin_memory=True)
+    hq.copy_(Q.T)
+    hcs = torch.empty_like(cs, device="cpu").pin_memory()
+    hcs.copy_(cs)
+    hfn = getattr(lib, f"symeig_apply_givens_{args.dtype}")
+    h2 = pkg.Handle(local)
+
+    def e2e_step():
+        rc = hfn(h2.ptr, ctypes.c_void_p(hq.data_ptr()), m, m, n, ctypes.c_void_p(hcs.data_ptr()), k)
+        if rc != 0:
+            raise RuntimeError(f"symeig_apply_givens_{args.dtype} -> {rc}")
+    e2e_step()
+    if world > 1:
+        dist.barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        e2e_step()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    esz = 8 if args.dtype == "f64" else 4
+    e2e = {"value": round(fl * world / e2e_s / 1e9, 3), "unit": "GFLOP/s",
+           "h2d_bytes_per_step": int(m * n * esz + (n - 1) * k * 2 * esz),
+           "d2h_bytes_per_step": int(m * n * esz), "ms_per_step": round(e2e_s * 1e3, 3),
+           "entry_point": f"symeig_apply_givens_{args.dtype} (host pointers, pinned)"}
+    del hq, hcs
+    h2.close()
+
+    extras = {}
+    if rank == 0 and not args.no_extras:
+        extras = side_measurements(pkg, lib, h, dev, stream, args)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        gf, rows, dt, shape = cpu_wave_gflops(m, n, k, args.dtype, threads, target_s=8.0)
+        cpu = {"value": round(gf, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+               "sample": (f"C port of the reference wave kernel, {threads} threads, {shape[0]} of {m} rows "
+                          f"x {shape[1]} cols, k={shape[2]}, {dt:.1f} s")}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "GFLOP/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms_per_step, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.dtype,
+            "data": "synthetic (seeded U[-1,1) Q, (cos t, sin t) rotations, t ~ U[0, 2pi))",
+            "config": {"workload": WORKLOAD, "m": m, "n": n, "k": k,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (Q = %.2f GB)" % (m * n * esz / 1e9)},
+            "roofline": {"bound": "fp64" if args.dtype == "f64" else "fp32", "achieved": round(achieved, 4),
+                         "peak": round(peak, 4), "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
+                         "frac_of_givens_ceiling": round(achieved / peak / 0.75, 4),
+                         "peak_source": "measured now by symeig_measure_fma_peak (FMA = 2 flops); "
+                                        "a Givens rotation-row is 4 FMA-pipe ops for 6 counted flops, so 0.75 is the ceiling",
+                         "traffic": read_traffic(), "algorithmic_bytes": algo_bytes,
+                         "kernel_ms": round(per_launch_ms, 3)},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+        }
+        line.update(extras)
+        print(json.dumps(line), flush=True)
+    h.close()
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def side_measurements(pkg, lib, h, dev, stream, args):
+    """FP32 apply on the same workload and the n=2000 solve (README example) for context."""
+    import ctypes
+    import torch
+    out = {}
+    m, n, k = args.m, args.n, args.k
+    if args.dtype == "f64":
+        Q, cs = make_inputs(m, n, k, "f32", seed=99, device=dev)
+        fn = lib.symeig_apply_givens_f32_dev
+        for _ in range(3):
+            fn(h.ptr, ctypes.c_void_p(Q.data_ptr()), Q.stride(1), m, n, ctypes.c_void_p(cs.data_ptr()), k)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(5):
+            fn(h.ptr, ctypes.c_void_p(Q.data_ptr()), Q.stride(1), m, n, ctypes.c_void_p(cs.data_ptr()), k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 5
+        peak32 = pkg._lib.measure_fma_peak(dev.index, fp64=False)
+        gf = flops_per_step(m, n, k) / (ms * 1e-3) / 1e9
+        out["f32_apply"] = {"value": round(gf, 1), "unit": "GFLOP/s", "ms_per_step": round(ms, 3),
+                            "frac_of_fp32_peak": round(gf / 1e3 / peak32, 4), "fp32_peak_tflops": round(peak32, 2)}
+        del Q, cs
+    # qr_algorithm! at n = 2000, d = 1:n, e ~ U[0,1) seed 0 (README.md:65-77)
+    nn = 2000
+    rng = np.random.default_rng(0)
+    d, e = np.arange(1, nn + 1, dtype=np.float64), rng.random(nn - 1)
+    H = pkg.SymTridiagonal(d.copy(), e.copy())
+    Qh = np.asfortranarray(np.eye(nn))
+    h.set_stream(None)
+    t0 = time.perf_counter()
+    _, conv, it = pkg.qr_algorithm_(H, Qh, handle=h)
+    dt = time.perf_counter() - t0
+    st = h.stats()
+    h.set_stream(stream.cuda_stream)
+    T = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    resid = float(np.linalg.norm(T @ Qh - Qh * H.dv) / np.linalg.norm(T))
+    orth = float(np.linalg.norm(Qh.T @ Qh - np.eye(nn)))
+    out["solve_n2000"] = {"seconds": round(dt, 3), "converged": conv, "iter": it,
+                          "chase_ms": round(st["chase_ms"], 1), "apply_ms": round(st["apply_ms"], 1),
+                          "rotations": st["rotations"], "resid_rel": resid, "orth": orth}
+    return out
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

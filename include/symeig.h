@@ -1,0 +1,140 @@
+/*
+ * symeig.h -- C ABI of libsymeig.so, the GB300 (sm_103a) implementation of
+ * SymmetricEigenProblem.jl's eigensolver hot path.
+ *
+ * Every entry point returns an int status: 0 = success, > 0 = argument error (nothing was
+ * touched), < 0 = device error.  No C++ exception crosses this boundary.  Matrices are
+ * column-major with an explicit leading dimension, exactly as Julia stores them.  A handle
+ * owns one device, one CUDA stream and grow-only scratch buffers; use one handle per host
+ * thread.
+ *
+ * Reference interfaces replaced (paths inside the SymmetricEigenProblem.jl project):
+ *   symeig_qr_*            qr_algorithm!(H::SymTridiagonal, Q, max_layers, tol, maxiter)
+ *                          src/bulge_chasing.jl:146  -> (H, converged, iter)
+ *   symeig_apply_givens_*  bulk_wave_order_2x2_rmul!(A, givens)  src/wave.jl:62 and
+ *                          bulk_wave_order_2x2_rmul_parallel!(A, givens)  src/wave.jl:36
+ *   symeig_eigen_decomp_*  eigen_decomp!(H)  src/bulge_chasing.jl:290-299
+ */
+#ifndef SYMEIG_H
+#define SYMEIG_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------- */
+#define SYMEIG_OK                 0
+#define SYMEIG_ERR_NULL           1   /* a required pointer is NULL                       */
+#define SYMEIG_ERR_SIZE           2   /* n < 1, m < 0, k < 0, or a size overflows         */
+#define SYMEIG_ERR_LD             3   /* leading dimension smaller than the row count     */
+#define SYMEIG_ERR_LAYERS         4   /* max_layers < 1                                   */
+#define SYMEIG_ERR_HANDLE         5   /* invalid handle                                   */
+#define SYMEIG_ERR_CUDA          -1   /* a CUDA runtime call failed                       */
+#define SYMEIG_ERR_NOMEM         -2   /* device or pinned host allocation failed          */
+#define SYMEIG_ERR_TIMEOUT       -3   /* a bounded device wait ran out (kernel returned)  */
+#define SYMEIG_ERR_DEVICE        -4   /* a kernel reported an internal error              */
+
+typedef struct symeig_context* symeig_handle;
+
+/* Statistics of the last solve or apply on a handle. */
+typedef struct {
+    int64_t iterations;      /* QR sweeps (the reference's iter)                          */
+    int64_t flushes;         /* bulk applications of the rotation buffer                  */
+    int64_t rotations;       /* non-padding rotations recorded by the chase               */
+    int64_t applied_rotation_rows; /* rotations x rows of Q the apply kernels processed   */
+    double  chase_ms;        /* device time of the chase kernels                          */
+    double  apply_ms;        /* device time of the table-build + apply kernels            */
+    double  total_ms;        /* wall time of the call                                     */
+    int64_t early_flushes;   /* flushes ended early to keep exact rotation order (see below)  */
+    int64_t wave_launches;   /* launches of the wave-window Givens kernel                 */
+    double  wave_kernel_ms;  /* their summed device time (only with kernel timing on)     */
+} symeig_stats;
+
+/* Create a handle bound to CUDA device `device`.  Replaces nothing in the reference (the
+ * Julia code has no device state); the Julia binding creates one per task. */
+int symeig_create(symeig_handle* out, int device);
+int symeig_destroy(symeig_handle h);
+/* The stream the *_dev entry points run on: a cudaStream_t, where NULL is the legacy default
+ * stream.  A new handle uses a non-blocking stream of its own; symeig_get_stream returns the
+ * current one (save it to restore it later). */
+int symeig_set_stream(symeig_handle h, void* stream);
+int symeig_get_stream(symeig_handle h, void** stream);
+int symeig_get_stats(symeig_handle h, symeig_stats* out);
+/* Rotation placement of the qr driver.  1 (default): every rotation of a sweep goes to one
+ * grid layer, so the layer-major (wave) order of a flush is exactly the order the chase
+ * produced the rotations; eigenvalues and the sweep sequence are the reference's.  0: the
+ * reference's placement, grid[i, ++layer_thickness[i]] (src/bulge_chasing.jl:61-63,
+ * 137-139), whose wave order differs from the chase's order when a split block re-merges
+ * within a flush (Q then loses accuracy in the reference too).  No reference counterpart. */
+int symeig_set_exact_order(symeig_handle h, int32_t exact_order);
+/* Record CUDA events around every wave-kernel launch so symeig_get_stats can report their
+ * device time (wave_kernel_ms).  Off by default.  symeig_get_stats waits for the last
+ * marked launch.  No reference counterpart (the reference times with BenchmarkTools). */
+int symeig_set_kernel_timing(symeig_handle h, int32_t on);
+/* FMA throughput of device `device` now, in TFLOP/s (an FMA = 2 flops), FP64 when fp64 != 0
+ * else FP32: the roofline denominator of the Givens kernels.  Runs ~10 ms.  No reference
+ * counterpart (the README compares with LinearAlgebra.peakflops(), README.md:28-31). */
+int symeig_measure_fma_peak(int device, int32_t fp64, double* tflops);
+const char* symeig_status_string(int status);
+/* Device properties the library tuned for (SM count, FP64/FP32 launch shapes). */
+int symeig_device_info(symeig_handle h, int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);
+
+/* ---- qr_algorithm!  (src/bulge_chasing.jl:146-288) ---------------------------------- *
+ * d[n] (diagonal) and e[n-1] (off-diagonal) are overwritten: d holds the eigenvalues,
+ * unsorted, as H.dv does in the reference; e holds the deflated off-diagonal.
+ * Q (m x n, column-major, leading dimension ldq >= m) is overwritten with Q * prod(G).
+ * Q == NULL (with m == 0) computes eigenvalues only.  max_layers, tol and maxiter mean what
+ * they mean in the reference (defaults there: 128, eps(Float64), 100n).  On return
+ * *converged is 0 when iter exceeded maxiter (the reference's (H, false, iter)), and the
+ * rotations of the unfinished flush are not applied to Q, as in the reference.
+ * Unlike the reference, odd n is accepted (the even-n assert, src/bulge_chasing.jl:155,
+ * exists only for the reference's fused kernels).
+ * Host-pointer variants copy to the device and back; *_dev variants take device pointers
+ * and run on the handle's stream (they return after the solve has finished). */
+int symeig_qr_f64(symeig_handle h, double* d, double* e, int64_t n,
+                  double* Q, int64_t ldq, int64_t m,
+                  int32_t max_layers, double tol, int64_t maxiter,
+                  int32_t* converged, int64_t* iter);
+int symeig_qr_f64_dev(symeig_handle h, double* d, double* e, int64_t n,
+                      double* Q, int64_t ldq, int64_t m,
+                      int32_t max_layers, double tol, int64_t maxiter,
+                      int32_t* converged, int64_t* iter);
+/* FP32-Q variant: the chase is FP64, each (c,s) is rounded to float, Q is float. */
+int symeig_qr_f64_q32(symeig_handle h, double* d, double* e, int64_t n,
+                      float* Q, int64_t ldq, int64_t m,
+                      int32_t max_layers, double tol, int64_t maxiter,
+                      int32_t* converged, int64_t* iter);
+int symeig_qr_f64_q32_dev(symeig_handle h, double* d, double* e, int64_t n,
+                          float* Q, int64_t ldq, int64_t m,
+                          int32_t max_layers, double tol, int64_t maxiter,
+                          int32_t* converged, int64_t* iter);
+
+/* ---- bulk_wave_order_2x2_rmul!  (src/wave.jl:36-162) ---------------------------------- *
+ * A (m x n, column-major, lda >= m) <- A * prod of the (n-1) x k grid of rotations cs,
+ * in the reference's wave order (equivalently: for L in 1:k, for i in 1:n-1,
+ * rmul!(A, G[i,L]), src/simple_givens.jl:53-65).  cs uses Julia's Matrix{Tuple{T,T}}
+ * layout: rotation (i,L) (0-based) has c at cs[2*(i + L*(n-1))] and s at the next slot.
+ * Unlike the reference, any n >= 1 and any k >= 0 are accepted (the reference asserts odd
+ * n-1 and even k, src/wave.jl:65-66, and silently needs k <= n-1). */
+int symeig_apply_givens_f64(symeig_handle h, double* A, int64_t lda, int64_t m, int64_t n,
+                            const double* cs, int64_t k);
+int symeig_apply_givens_f32(symeig_handle h, float* A, int64_t lda, int64_t m, int64_t n,
+                            const float* cs, int64_t k);
+int symeig_apply_givens_f64_dev(symeig_handle h, double* A, int64_t lda, int64_t m, int64_t n,
+                                const double* cs, int64_t k);
+int symeig_apply_givens_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t m, int64_t n,
+                                const float* cs, int64_t k);
+
+/* ---- eigen_decomp!  (src/bulge_chasing.jl:290-299) ----------------------------------- *
+ * Q (n x n, ldq >= n) is set to the identity, then qr_algorithm! runs with the default
+ * max_layers = 128, tol = eps, maxiter = 100n.  d/e overwritten as in symeig_qr_f64. */
+int symeig_eigen_decomp_f64(symeig_handle h, double* d, double* e, int64_t n,
+                            double* Q, int64_t ldq, int32_t* converged, int64_t* iter);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SYMEIG_H */

@@ -1,0 +1,208 @@
+"""Host-side mirror of SymmetricEigenProblem.jl's public functions for the hot path.
+
+Same names (with ``!`` spelled ``_``), argument meaning and results as the reference:
+
+  qr_algorithm_(H, Q, max_layers=128, tol=eps, maxiter=100n) -> (H, converged, iter)
+      src/bulge_chasing.jl:146-288
+  bulk_wave_order_2x2_rmul_(A, givens)            src/wave.jl:62-162
+  bulk_wave_order_2x2_rmul_parallel_(A, givens)   src/wave.jl:36-60
+  eigen_decomp_(H) -> (eigenvalues, Q)            src/bulge_chasing.jl:290-299
+
+Every call goes to libsymeig.so on the GPU.  Arrays may be numpy (host buffers: the library
+copies them to the device and back) or CUDA torch tensors (device buffers, no copies).
+Matrices are column-major like Julia's: a numpy array in Fortran order, or a torch tensor
+with stride(0) == 1 (e.g. ``torch.empty(n, m).T``).  A rotation grid ``givens`` is the
+Julia ``Matrix{Tuple{T,T}}``: shape (n-1, k, 2), entry [i, L] = (c, s), with memory laid out
+as Julia lays it out (pair, then i, then L) -- ``givens_buffer`` builds one.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import default_handle, Handle, c_i32, c_i64
+
+try:  # torch is optional for host-buffer use
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+EPS64 = float(np.finfo(np.float64).eps)
+
+
+@dataclass
+class SymTridiagonal:
+    """LinearAlgebra.SymTridiagonal(dv, ev): dv (n,) and ev (n-1,) float64 (numpy or CUDA torch)."""
+    dv: object
+    ev: object
+
+    @property
+    def n(self) -> int:
+        return int(self.dv.shape[0])
+
+    def copy(self) -> "SymTridiagonal":
+        if _is_torch(self.dv):
+            return SymTridiagonal(self.dv.clone(), self.ev.clone())
+        return SymTridiagonal(np.array(self.dv, copy=True), np.array(self.ev, copy=True))
+
+    def dense(self) -> np.ndarray:
+        d = _to_numpy(self.dv)
+        e = _to_numpy(self.ev)
+        return np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+
+
+def _is_torch(x) -> bool:
+    return torch is not None and isinstance(x, torch.Tensor)
+
+
+def _to_numpy(x):
+    return x.detach().cpu().numpy() if _is_torch(x) else np.asarray(x)
+
+
+def _colmajor_info(A):
+    """(pointer, ld, m, n, dtype-name, on_device) of a column-major matrix."""
+    if _is_torch(A):
+        if not A.is_cuda:
+            raise ValueError("torch matrices must live on a CUDA device")
+        if A.dim() != 2:
+            raise ValueError("matrix must be 2-D")
+        m, n = A.shape
+        if n > 0 and m > 1 and A.stride(0) != 1:
+            raise ValueError("matrix must be column-major (stride(0) == 1), e.g. torch.empty(n, m).T")
+        ld = A.stride(1) if n > 1 else max(m, 1)
+        dt = {torch.float64: "f64", torch.float32: "f32"}.get(A.dtype)
+        if dt is None:
+            raise TypeError(f"unsupported dtype {A.dtype}")
+        return A.data_ptr(), max(ld, m, 1), m, n, dt, True
+    if not isinstance(A, np.ndarray) or A.ndim != 2:
+        raise ValueError("matrix must be a 2-D numpy array or CUDA torch tensor")
+    m, n = A.shape
+    if not A.flags.writeable or (m > 1 and n > 0 and A.strides[0] != A.itemsize):
+        raise ValueError("matrix must be a writeable column-major (Fortran-ordered) array")
+    ld = A.strides[1] // A.itemsize if n > 1 else max(m, 1)
+    dt = {np.dtype(np.float64): "f64", np.dtype(np.float32): "f32"}.get(A.dtype)
+    if dt is None:
+        raise TypeError(f"unsupported dtype {A.dtype}")
+    return A.ctypes.data, max(ld, m, 1), m, n, dt, False
+
+
+def givens_buffer(n_minus_1: int, k: int, dtype=np.float64) -> np.ndarray:
+    """An uninitialised Julia-layout Matrix{Tuple{T,T}} of shape (n-1, k, 2)."""
+    return np.empty((k, n_minus_1, 2), dtype=dtype).transpose(1, 0, 2)
+
+
+def _givens_ptr(givens, dtype_name: str, on_device: bool):
+    """Pointer to a Julia-layout (n-1, k, 2) rotation grid, plus a keep-alive object."""
+    if _is_torch(givens):
+        if not on_device or not givens.is_cuda:
+            raise ValueError("givens and A must both be host arrays or both CUDA tensors")
+        g = givens.permute(1, 0, 2).contiguous()  # (k, n-1, 2) row-major == Julia layout
+        want = torch.float64 if dtype_name == "f64" else torch.float32
+        if g.dtype != want:
+            raise TypeError("givens must have the dtype of A")
+        return g.data_ptr(), g, int(givens.shape[1])
+    g = np.asarray(givens)
+    if on_device:
+        raise ValueError("givens and A must both be host arrays or both CUDA tensors")
+    want = np.float64 if dtype_name == "f64" else np.float32
+    if g.dtype != want:
+        raise TypeError("givens must have the dtype of A")
+    if g.ndim != 3 or g.shape[2] != 2:
+        raise ValueError("givens must have shape (n-1, k, 2)")
+    buf = np.ascontiguousarray(g.transpose(1, 0, 2))
+    return buf.ctypes.data, buf, int(g.shape[1])
+
+
+def bulk_wave_order_2x2_rmul_(A, givens, handle: Handle | None = None) -> None:
+    """A <- A * prod(G) for the (n-1) x k rotation grid, in the reference's wave order
+    (src/wave.jl:62-162).  Unlike the reference, any n and any k are accepted."""
+    h = handle or default_handle(A.device.index if _is_torch(A) else 0)
+    ptr, ld, m, n, dt, dev = _colmajor_info(A)
+    gn = int(givens.shape[0])
+    if n >= 2 and gn != n - 1:
+        raise ValueError(f"givens has {gn} rows, expected n-1 = {n - 1}")
+    if n < 2 or m == 0 or int(givens.shape[1]) == 0:
+        return None
+    gptr, keep, k = _givens_ptr(givens, dt, dev)
+    name = f"symeig_apply_givens_{dt}" + ("_dev" if dev else "")
+    if dev:  # run on torch's current stream: ordered after the producers of A and givens
+        with h.on_stream(torch.cuda.current_stream(A.device).cuda_stream):
+            h.call(name, ctypes.c_void_p(ptr), ld, m, n, ctypes.c_void_p(gptr), k)
+    else:
+        h.call(name, ctypes.c_void_p(ptr), ld, m, n, ctypes.c_void_p(gptr), k)
+    if dev:
+        # keep the temporary Julia-layout copy alive until the kernels that read it finish
+        torch.cuda.current_stream(A.device).synchronize()
+    del keep
+    return None
+
+
+def bulk_wave_order_2x2_rmul_parallel_(A, givens, handle: Handle | None = None) -> None:
+    """src/wave.jl:36-60: the row-slab threaded variant.  On the GPU every row already has
+    its own thread, so this is the same call."""
+    return bulk_wave_order_2x2_rmul_(A, givens, handle)
+
+
+def qr_algorithm_(H: SymTridiagonal, Q=None, max_layers: int = 128, tol: float | None = None,
+                  maxiter: int | None = None, handle: Handle | None = None,
+                  exact_order: bool = True):
+    """qr_algorithm!(H, Q, max_layers=128, tol=eps(T), maxiter=100n) -> (H, converged, iter)
+    (src/bulge_chasing.jl:146-288).  H.dv becomes the (unsorted) eigenvalues, Q <- Q*prod(G).
+    Q may be None (eigenvalues only), float64 or float32 (the FP32-Q variant: FP64 chase,
+    (c,s) rounded to float).  exact_order=False places rotations in the grid as the reference
+    does (grid[i, ++layer_thickness[i]]), which loses accuracy in Q when a split block
+    re-merges within a flush; the default places each sweep at one layer so Q is exact."""
+    n = H.n
+    tol = EPS64 if tol is None else float(tol)
+    maxiter = 100 * n if maxiter is None else int(maxiter)
+    dev = _is_torch(H.dv)
+    if dev:
+        if not (H.dv.is_cuda and H.ev.is_cuda) or H.dv.dtype != torch.float64 or H.ev.dtype != torch.float64:
+            raise TypeError("H.dv / H.ev must be CUDA float64 tensors")
+        if not (H.dv.is_contiguous() and H.ev.is_contiguous()):
+            raise ValueError("H.dv / H.ev must be contiguous")
+        dptr, eptr = H.dv.data_ptr(), (H.ev.data_ptr() if H.ev.numel() else None)
+    else:
+        for a in (H.dv, H.ev):
+            if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous or not a.flags.writeable:
+                raise TypeError("H.dv / H.ev must be writeable contiguous float64 numpy arrays")
+        dptr, eptr = H.dv.ctypes.data, (H.ev.ctypes.data if H.ev.size else None)
+    if H.ev.shape[0] != max(n - 1, 0):
+        raise ValueError("ev must have n-1 entries")
+    if Q is None:
+        qptr, ld, m, dt = None, 1, 0, "f64"
+    else:
+        qptr, ld, m, nq, dt, qdev = _colmajor_info(Q)
+        if qdev != dev:
+            raise ValueError("H and Q must both be host arrays or both CUDA tensors")
+        if nq != n:
+            raise ValueError(f"Q has {nq} columns, expected n = {n}")
+    h = handle or default_handle(H.dv.device.index if dev else 0)
+    conv, it = c_i32(), c_i64()
+    name = "symeig_qr_f64" + ("_q32" if dt == "f32" else "") + ("_dev" if dev else "")
+    h.set_exact_order(exact_order)
+    try:
+        args = (ctypes.c_void_p(dptr), ctypes.c_void_p(eptr), n, ctypes.c_void_p(qptr), ld, m,
+                int(max_layers), tol, maxiter, ctypes.byref(conv), ctypes.byref(it))
+        if dev:  # ordered after torch's pending work on H and Q; returns when the solve is done
+            with h.on_stream(torch.cuda.current_stream(H.dv.device).cuda_stream):
+                h.call(name, *args)
+        else:
+            h.call(name, *args)
+    finally:
+        h.set_exact_order(True)
+    return H, bool(conv.value), int(it.value)
+
+
+def eigen_decomp_(H: SymTridiagonal, handle: Handle | None = None):
+    """eigen_decomp!(H) (src/bulge_chasing.jl:290-299): Q = I, qr_algorithm!, returns
+    (eigenvalues, Q).  The reference returns Diagonal(H.dv); here the 1-D array H.dv."""
+    n = H.n
+    if _is_torch(H.dv):
+        Q = torch.eye(n, dtype=torch.float64, device=H.dv.device).T  # column-major view
+    else:
+        Q = np.asfortranarray(np.eye(n))
+    _, converged, iters = qr_algorithm_(H, Q, handle=handle)
+    return H.dv, Q

@@ -1,0 +1,558 @@
+// api.cu -- the C ABI of libsymeig.so (declared in include/symeig.h) and the host driver of
+// the device eigensolver.
+//
+// qr driver.  The reference's outer loop (src/bulge_chasing.jl:166-284) alternates a serial
+// chase that fills a (n-1) x max_layers rotation buffer with a bulk application of that
+// buffer to Q.  Here the chase is a one-warp kernel on a side stream and the apply is the
+// wave-window kernel on the main stream.  The rotation grid is double-buffered: the chase of
+// flush f+1 runs while flush f is applied, since the chase reads only (d, e) and the apply
+// reads only the grid and Q.  After each chase the host reads its 100-byte status (pinned
+// memory) to learn whether to apply, stop (converged) or give up (maxiter), exactly the
+// three exits of the reference.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "symeig.h"
+#include "symeig_common.cuh"
+
+using namespace symeig;
+
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    cudaError_t ensure(size_t want)
+    {
+        if (want <= bytes) return cudaSuccess;
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+        cudaError_t e = cudaMalloc(&ptr, want);
+        if (e == cudaSuccess) bytes = want;
+        return e;
+    }
+    void release()
+    {
+        if (ptr) cudaFree(ptr);
+        ptr = nullptr;
+        bytes = 0;
+    }
+};
+
+struct symeig_context {
+    int device = 0;
+    int sm_count = 0, cc_major = 0, cc_minor = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;       // main (apply) stream
+    cudaStream_t chase_stream = nullptr; // side stream for the chase
+    cudaEvent_t ev_chased[2] = {nullptr, nullptr};
+    cudaEvent_t ev_consumed[2] = {nullptr, nullptr};
+    cudaEvent_t ev_main = nullptr;
+    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs;
+    int32_t exact_order = 1;  // rotation placement of the qr driver
+    ChaseState* h_state = nullptr;  // pinned
+    std::vector<cudaEvent_t> timing;  // pool of timing events
+    symeig_stats stats{};
+    // optional per-launch timing of the wave kernel (symeig_set_kernel_timing)
+    bool kernel_timing = false;
+    std::vector<cudaEvent_t> kpool;
+    size_t kused = 0;
+    bool kpending = false;
+};
+
+namespace {
+
+int cuda_status(cudaError_t e)
+{
+    if (e == cudaSuccess) return SYMEIG_OK;
+    if (e == cudaErrorMemoryAllocation) return SYMEIG_ERR_NOMEM;
+    return SYMEIG_ERR_CUDA;
+}
+
+#define CK(call)                                        \
+    do {                                                \
+        cudaError_t _e = (call);                        \
+        if (_e != cudaSuccess) return cuda_status(_e);  \
+    } while (0)
+
+int check_handle(symeig_handle h)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    if (cudaSetDevice(h->device) != cudaSuccess) return SYMEIG_ERR_CUDA;
+    return SYMEIG_OK;
+}
+
+bool mul_overflows(int64_t a, int64_t b)
+{
+    return a > 0 && b > 0 && a > INT64_MAX / b;
+}
+
+int validate_matrix(const void* A, int64_t lda, int64_t m, int64_t n)
+{
+    if (m < 0 || n < 0) return SYMEIG_ERR_SIZE;
+    if (m > 0 && n > 0 && !A) return SYMEIG_ERR_NULL;
+    if (m > 0 && lda < m) return SYMEIG_ERR_LD;
+    if (mul_overflows(lda, n)) return SYMEIG_ERR_SIZE;
+    return SYMEIG_OK;
+}
+
+cudaEvent_t timing_event(symeig_handle h, size_t idx)
+{
+    while (h->timing.size() <= idx) {
+        cudaEvent_t ev;
+        if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
+        h->timing.push_back(ev);
+    }
+    return h->timing[idx];
+}
+
+cudaEvent_t kernel_event(symeig_handle h)
+{
+    if (h->kused == h->kpool.size()) {
+        cudaEvent_t ev;
+        if (cudaEventCreate(&ev) != cudaSuccess) return nullptr;
+        h->kpool.push_back(ev);
+    }
+    return h->kpool[h->kused++];
+}
+
+// Start a new call: statistics and kernel-timing marks refer to the last call only.
+void begin_call(symeig_handle h)
+{
+    std::memset(&h->stats, 0, sizeof(h->stats));
+    h->kused = 0;
+    h->kpending = false;
+}
+
+// Run every pass of one bulk apply of `layers` layers of `grid` to columns [c0, c0+n_loc).
+template <typename Tsrc, typename T>
+int apply_grid(symeig_handle h, T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t grid_rows,
+               const int32_t* thick, int64_t c0, int64_t n_loc, int64_t layers, cudaStream_t s)
+{
+    if (m <= 0 || n_loc < 2 || layers <= 0) return SYMEIG_OK;
+    const int64_t per = apply_layers_per_pass<T>();
+    CK(h->table.ensure(apply_table_bytes<T>(n_loc, per)));
+    for (int64_t L0 = 0; L0 < layers; L0 += per) {
+        ApplyPass pass{c0, n_loc, L0, std::min(per, layers - L0)};
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (h->kernel_timing) {
+            e0 = kernel_event(h);
+            e1 = kernel_event(h);
+            if (!e0 || !e1) return SYMEIG_ERR_CUDA;
+            h->kpending = true;
+        }
+        CK((apply_pass<Tsrc, T>(Q, ldq, m, grid, grid_rows, thick, pass, h->table.ptr, s, e0, e1)));
+        h->stats.wave_launches += 1;
+    }
+    h->stats.applied_rotation_rows += (n_loc - 1) * layers * m;
+    return SYMEIG_OK;
+}
+
+template <typename T>
+int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, int64_t m,
+           int32_t max_layers, double tol, int64_t maxiter, int32_t* converged, int64_t* iter)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!converged || !iter) return SYMEIG_ERR_NULL;
+    if (n < 1) return SYMEIG_ERR_SIZE;
+    if (!d || (n > 1 && !e)) return SYMEIG_ERR_NULL;
+    if (max_layers < 1) return SYMEIG_ERR_LAYERS;
+    if (Q == nullptr) m = 0;
+    rc = validate_matrix(Q, ldq, m, n);
+    if (rc) return rc;
+    const int64_t rows = n > 1 ? n - 1 : 1;
+    if (max_layers > (1 << 29) || mul_overflows(rows, (int64_t)max_layers * 32)) return SYMEIG_ERR_SIZE;
+    // exact-order placement can need more layers than the reference's capacity rule allows
+    const int32_t grid_layers = h->exact_order ? 2 * max_layers : max_layers;
+
+    auto t0 = std::chrono::steady_clock::now();
+    begin_call(h);
+    const size_t grid_bytes = (size_t)rows * grid_layers * 2 * sizeof(double);
+    for (int b = 0; b < 2; ++b) {
+        CK(h->grid[b].ensure(grid_bytes));
+        CK(h->thick[b].ensure((size_t)n * sizeof(int32_t)));
+        CK(h->place[b].ensure((size_t)n * sizeof(int32_t)));
+    }
+    CK(h->state.ensure(sizeof(ChaseState)));
+
+    ChaseState init{};
+    init.n = n;
+    init.start = 1;
+    init.last_block_ends_at = n;
+    init.iter = 0;
+    init.maxiter = maxiter;
+    init.tol = tol;
+    init.max_layers = max_layers;
+    init.grid_layers = grid_layers;
+    init.exact_order = h->exact_order;
+    init.status = CHASE_RUNNING;
+    ChaseState* dstate = (ChaseState*)h->state.ptr;
+
+    cudaStream_t ms = h->stream, cs = h->chase_stream;
+    // the chase must see whatever the caller enqueued on the main stream (d, e, Q writes)
+    CK(cudaEventRecord(h->ev_main, ms));
+    CK(cudaStreamWaitEvent(cs, h->ev_main, 0));
+    CK(cudaMemcpyAsync(dstate, &init, sizeof(init), cudaMemcpyHostToDevice, cs));
+    // the memcpy above reads a stack object: make it complete before returning from scope
+    CK(cudaStreamSynchronize(cs));
+
+    size_t tev = 0;
+    double chase_ms = 0.0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> apply_marks;
+    int32_t conv = 1;
+    int64_t flush = 0;
+    int result = SYMEIG_OK;
+    for (;; ++flush) {
+        const int b = (int)(flush & 1);
+        if (flush >= 2) CK(cudaStreamWaitEvent(cs, h->ev_consumed[b], 0));
+        cudaEvent_t c0 = timing_event(h, tev++), c1 = timing_event(h, tev++);
+        if (!c0 || !c1) return SYMEIG_ERR_CUDA;
+        CK(cudaEventRecord(c0, cs));
+        CK(launch_chase(dstate, d, e, (double*)h->grid[b].ptr, (int32_t*)h->thick[b].ptr,
+                        (int32_t*)h->place[b].ptr, cs));
+        CK(cudaEventRecord(c1, cs));
+        CK(cudaMemcpyAsync(h->h_state, dstate, sizeof(ChaseState), cudaMemcpyDeviceToHost, cs));
+        CK(cudaEventRecord(h->ev_chased[b], cs));
+        CK(cudaEventSynchronize(h->ev_chased[b]));
+        float ms_chase = 0.f;
+        CK(cudaEventElapsedTime(&ms_chase, c0, c1));
+        chase_ms += ms_chase;
+        const ChaseState st = *h->h_state;
+        if (st.status == CHASE_MAXITER) { conv = 0; break; }
+        if (st.status == CHASE_CONVERGED) break;
+        if (st.status != CHASE_FLUSH) { result = SYMEIG_ERR_DEVICE; break; }
+        h->stats.flushes += 1;
+        if (m > 0) {
+            CK(cudaStreamWaitEvent(ms, h->ev_chased[b], 0));
+            cudaEvent_t a0 = timing_event(h, tev++), a1 = timing_event(h, tev++);
+            if (!a0 || !a1) return SYMEIG_ERR_CUDA;
+            CK(cudaEventRecord(a0, ms));
+            const int64_t c_lo = st.min_from - 1;          // 0-based first column touched
+            const int64_t n_loc = st.max_to - c_lo;         // columns from..to of every sweep
+            rc = apply_grid<double, T>(h, Q, ldq, m, (const double*)h->grid[b].ptr, rows,
+                                       (const int32_t*)h->place[b].ptr, c_lo, n_loc,
+                                       st.max_thickness, ms);
+            if (rc) return rc;
+            CK(cudaEventRecord(a1, ms));
+            apply_marks.emplace_back(a0, a1);
+            CK(cudaEventRecord(h->ev_consumed[b], ms));
+        } else {
+            CK(cudaEventRecord(h->ev_consumed[b], cs));
+        }
+    }
+    CK(cudaEventRecord(h->ev_main, cs));
+    CK(cudaStreamWaitEvent(ms, h->ev_main, 0));
+    CK(cudaStreamSynchronize(ms));
+    double apply_ms = 0.0;
+    for (auto& pr : apply_marks) {
+        float x = 0.f;
+        CK(cudaEventElapsedTime(&x, pr.first, pr.second));
+        apply_ms += x;
+    }
+    const ChaseState fin = *h->h_state;
+    *converged = conv;
+    *iter = fin.iter;
+    h->stats.iterations = fin.iter;
+    h->stats.rotations = fin.total_rotations;
+    h->stats.early_flushes = fin.early_flushes;
+    h->stats.chase_ms = chase_ms;
+    h->stats.apply_ms = apply_ms;
+    h->stats.total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return result;
+}
+
+template <typename T>
+int qr_host(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, int64_t m,
+            int32_t max_layers, double tol, int64_t maxiter, int32_t* converged, int64_t* iter)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 1) return SYMEIG_ERR_SIZE;
+    if (!d || (n > 1 && !e) || !converged || !iter) return SYMEIG_ERR_NULL;
+    if (Q == nullptr) m = 0;
+    rc = validate_matrix(Q, ldq, m, n);
+    if (rc) return rc;
+    auto t0 = std::chrono::steady_clock::now();
+    const int64_t ne = n > 1 ? n - 1 : 1;
+    CK(h->d.ensure((size_t)n * sizeof(double)));
+    CK(h->e.ensure((size_t)ne * sizeof(double)));
+    T* dq = nullptr;
+    if (m > 0) {
+        CK(h->q.ensure((size_t)m * n * sizeof(T)));
+        dq = (T*)h->q.ptr;
+    }
+    cudaStream_t s = h->stream;
+    CK(cudaMemcpyAsync(h->d.ptr, d, n * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (n > 1) CK(cudaMemcpyAsync(h->e.ptr, e, (n - 1) * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (m > 0)
+        CK(cudaMemcpy2DAsync(dq, m * sizeof(T), Q, ldq * sizeof(T), m * sizeof(T), n,
+                             cudaMemcpyHostToDevice, s));
+    rc = qr_dev<T>(h, (double*)h->d.ptr, (double*)h->e.ptr, n, dq, m, m, max_layers, tol, maxiter,
+                   converged, iter);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(d, h->d.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (n > 1) CK(cudaMemcpyAsync(e, h->e.ptr, (n - 1) * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (m > 0)
+        CK(cudaMemcpy2DAsync(Q, ldq * sizeof(T), dq, m * sizeof(T), m * sizeof(T), n,
+                             cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    h->stats.total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return SYMEIG_OK;
+}
+
+template <typename T>
+int apply_dev(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T* cs, int64_t k)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (k < 0 || n < 0) return SYMEIG_ERR_SIZE;
+    rc = validate_matrix(A, lda, m, n);
+    if (rc) return rc;
+    if (n >= 2 && k > 0 && !cs) return SYMEIG_ERR_NULL;
+    if (mul_overflows(n, k * 2)) return SYMEIG_ERR_SIZE;
+    begin_call(h);
+    if (m == 0 || n < 2 || k == 0) return SYMEIG_OK;
+    return apply_grid<T, T>(h, A, lda, m, cs, n - 1, nullptr, 0, n, k, h->stream);
+}
+
+template <typename T>
+int apply_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T* cs, int64_t k)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (k < 0 || n < 0) return SYMEIG_ERR_SIZE;
+    rc = validate_matrix(A, lda, m, n);
+    if (rc) return rc;
+    if (n >= 2 && k > 0 && !cs) return SYMEIG_ERR_NULL;
+    if (m == 0 || n < 2 || k == 0) return SYMEIG_OK;
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = h->stream;
+    CK(h->q.ensure((size_t)m * n * sizeof(T)));
+    const size_t cs_bytes = (size_t)(n - 1) * k * 2 * sizeof(T);
+    CK(h->cs.ensure(cs_bytes));
+    CK(cudaMemcpyAsync(h->cs.ptr, cs, cs_bytes, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpy2DAsync(h->q.ptr, m * sizeof(T), A, lda * sizeof(T), m * sizeof(T), n,
+                         cudaMemcpyHostToDevice, s));
+    rc = apply_dev<T>(h, (T*)h->q.ptr, m, m, n, (const T*)h->cs.ptr, k);
+    if (rc) return rc;
+    CK(cudaMemcpy2DAsync(A, lda * sizeof(T), h->q.ptr, m * sizeof(T), m * sizeof(T), n,
+                         cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    h->stats.total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return SYMEIG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int symeig_create(symeig_handle* out, int device)
+{
+    if (!out) return SYMEIG_ERR_NULL;
+    *out = nullptr;
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || device < 0 || device >= count)
+        return SYMEIG_ERR_CUDA;
+    symeig_context* h = new (std::nothrow) symeig_context();
+    if (!h) return SYMEIG_ERR_NOMEM;
+    h->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->cc_major, cudaDevAttrComputeCapabilityMajor, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->cc_minor, cudaDevAttrComputeCapabilityMinor, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->chase_stream, cudaStreamNonBlocking);
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+        e = cudaEventCreateWithFlags(&h->ev_chased[b], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_consumed[b], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_main, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaMallocHost((void**)&h->h_state, sizeof(ChaseState));
+    if (e != cudaSuccess) {
+        symeig_destroy(h);
+        return cuda_status(e);
+    }
+    h->stream = h->own_stream;
+    *out = h;
+    return SYMEIG_OK;
+}
+
+int symeig_destroy(symeig_handle h)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    cudaSetDevice(h->device);
+    if (h->own_stream) cudaStreamSynchronize(h->own_stream);
+    if (h->chase_stream) cudaStreamSynchronize(h->chase_stream);
+    if (h->stream && h->stream != h->own_stream) cudaStreamSynchronize(h->stream);
+    for (int b = 0; b < 2; ++b) {
+        h->grid[b].release();
+        h->thick[b].release();
+        h->place[b].release();
+        if (h->ev_chased[b]) cudaEventDestroy(h->ev_chased[b]);
+        if (h->ev_consumed[b]) cudaEventDestroy(h->ev_consumed[b]);
+    }
+    h->table.release(); h->state.release(); h->d.release(); h->e.release();
+    h->q.release(); h->cs.release();
+    if (h->ev_main) cudaEventDestroy(h->ev_main);
+    for (cudaEvent_t ev : h->timing) cudaEventDestroy(ev);
+    for (cudaEvent_t ev : h->kpool) cudaEventDestroy(ev);
+    if (h->h_state) cudaFreeHost(h->h_state);
+    if (h->chase_stream) cudaStreamDestroy(h->chase_stream);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+    delete h;
+    return SYMEIG_OK;
+}
+
+int symeig_set_stream(symeig_handle h, void* stream)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    h->stream = (cudaStream_t)stream;  // NULL is the legacy default stream
+    return SYMEIG_OK;
+}
+
+int symeig_get_stream(symeig_handle h, void** stream)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    if (!stream) return SYMEIG_ERR_NULL;
+    *stream = (void*)h->stream;
+    return SYMEIG_OK;
+}
+
+int symeig_set_exact_order(symeig_handle h, int32_t exact_order)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    h->exact_order = exact_order ? 1 : 0;
+    return SYMEIG_OK;
+}
+
+int symeig_set_kernel_timing(symeig_handle h, int32_t on)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    h->kernel_timing = on != 0;
+    return SYMEIG_OK;
+}
+
+int symeig_get_stats(symeig_handle h, symeig_stats* out)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!out) return SYMEIG_ERR_NULL;
+    if (h->kpending) {
+        // wait for the last marked launch, then sum the wave-kernel durations of the call
+        CK(cudaEventSynchronize(h->kpool[h->kused - 1]));
+        double ms = 0.0;
+        for (size_t i = 0; i + 1 < h->kused; i += 2) {
+            float x = 0.f;
+            CK(cudaEventElapsedTime(&x, h->kpool[i], h->kpool[i + 1]));
+            ms += x;
+        }
+        h->stats.wave_kernel_ms = ms;
+        h->kpending = false;
+    }
+    *out = h->stats;
+    return SYMEIG_OK;
+}
+
+int symeig_device_info(symeig_handle h, int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    if (sm_count) *sm_count = h->sm_count;
+    if (cc_major) *cc_major = h->cc_major;
+    if (cc_minor) *cc_minor = h->cc_minor;
+    return SYMEIG_OK;
+}
+
+const char* symeig_status_string(int status)
+{
+    switch (status) {
+        case SYMEIG_OK: return "ok";
+        case SYMEIG_ERR_NULL: return "a required pointer is NULL";
+        case SYMEIG_ERR_SIZE: return "invalid size";
+        case SYMEIG_ERR_LD: return "leading dimension smaller than the row count";
+        case SYMEIG_ERR_LAYERS: return "max_layers must be >= 1";
+        case SYMEIG_ERR_HANDLE: return "invalid handle";
+        case SYMEIG_ERR_CUDA: return "CUDA runtime error";
+        case SYMEIG_ERR_NOMEM: return "out of memory";
+        case SYMEIG_ERR_TIMEOUT: return "bounded device wait timed out";
+        case SYMEIG_ERR_DEVICE: return "device kernel reported an error";
+        default: return "unknown status";
+    }
+}
+
+int symeig_qr_f64(symeig_handle h, double* d, double* e, int64_t n, double* Q, int64_t ldq,
+                  int64_t m, int32_t max_layers, double tol, int64_t maxiter, int32_t* converged,
+                  int64_t* iter)
+{
+    return qr_host<double>(h, d, e, n, Q, ldq, m, max_layers, tol, maxiter, converged, iter);
+}
+
+int symeig_qr_f64_dev(symeig_handle h, double* d, double* e, int64_t n, double* Q, int64_t ldq,
+                      int64_t m, int32_t max_layers, double tol, int64_t maxiter,
+                      int32_t* converged, int64_t* iter)
+{
+    return qr_dev<double>(h, d, e, n, Q, ldq, m, max_layers, tol, maxiter, converged, iter);
+}
+
+int symeig_qr_f64_q32(symeig_handle h, double* d, double* e, int64_t n, float* Q, int64_t ldq,
+                      int64_t m, int32_t max_layers, double tol, int64_t maxiter,
+                      int32_t* converged, int64_t* iter)
+{
+    return qr_host<float>(h, d, e, n, Q, ldq, m, max_layers, tol, maxiter, converged, iter);
+}
+
+int symeig_qr_f64_q32_dev(symeig_handle h, double* d, double* e, int64_t n, float* Q,
+                          int64_t ldq, int64_t m, int32_t max_layers, double tol,
+                          int64_t maxiter, int32_t* converged, int64_t* iter)
+{
+    return qr_dev<float>(h, d, e, n, Q, ldq, m, max_layers, tol, maxiter, converged, iter);
+}
+
+int symeig_apply_givens_f64(symeig_handle h, double* A, int64_t lda, int64_t m, int64_t n,
+                            const double* cs, int64_t k)
+{
+    return apply_host<double>(h, A, lda, m, n, cs, k);
+}
+
+int symeig_apply_givens_f32(symeig_handle h, float* A, int64_t lda, int64_t m, int64_t n,
+                            const float* cs, int64_t k)
+{
+    return apply_host<float>(h, A, lda, m, n, cs, k);
+}
+
+int symeig_apply_givens_f64_dev(symeig_handle h, double* A, int64_t lda, int64_t m, int64_t n,
+                                const double* cs, int64_t k)
+{
+    return apply_dev<double>(h, A, lda, m, n, cs, k);
+}
+
+int symeig_apply_givens_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t m, int64_t n,
+                                const float* cs, int64_t k)
+{
+    return apply_dev<float>(h, A, lda, m, n, cs, k);
+}
+
+int symeig_eigen_decomp_f64(symeig_handle h, double* d, double* e, int64_t n, double* Q,
+                            int64_t ldq, int32_t* converged, int64_t* iter)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 1) return SYMEIG_ERR_SIZE;
+    if (!Q) return SYMEIG_ERR_NULL;
+    if (ldq < n) return SYMEIG_ERR_LD;
+    for (int64_t j = 0; j < n; ++j)
+        for (int64_t i = 0; i < n; ++i) Q[i + j * ldq] = (i == j) ? 1.0 : 0.0;
+    const double eps = 2.220446049250313e-16;
+    return qr_host<double>(h, d, e, n, Q, ldq, n, 128, eps, 100 * n, converged, iter);
+}
+
+}  // extern "C"

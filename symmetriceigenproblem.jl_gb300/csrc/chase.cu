@@ -1,0 +1,305 @@
+// chase.cu -- the FP64 bulge-chase kernel: one flush of qr_algorithm! on the device.
+//
+// Restates, on one warp, the inner loop of qr_algorithm! (src/bulge_chasing.jl:166-279):
+// the deflation scan (:205-222, is_offdiagonal_small :7-8), the layer capacity rule
+// (:226-230), the Wilkinson shift (:239-265) and single_shift! (:11-144) with
+// get_rotation / LinearAlgebra.givensAlgorithm (src/simple_givens.jl:20-23).  The sweep is a
+// strict dependency chain and runs on lane 0; the O(n) scans (deflation, thickest column)
+// use all 32 lanes with ballots.  Rotations go to a Julia-layout (c,s) grid: at
+// grid[i, ++thickness[i]] as the reference records them, or (the default) at the sweep's
+// exact-order layer described at chase_kernel.
+//
+// Every floating-point operation is an explicit _rn intrinsic.  Inside single_shift! the
+// reference runs under @fastmath; this kernel and the CPU oracle fuse the first product of
+// each `u*a + v*b` (see symeig_common.cuh).  Outside it (givensAlgorithm, the shift, the
+// deflation test) the arithmetic is plain IEEE without contraction, as Julia compiles it.
+// Division and square root are the correctly rounded __ddiv_rn / __dsqrt_rn, so the kernel
+// reproduces the oracle's rotation stream bit for bit.
+//
+// The kernel never traps and never waits on another kernel: a flush ends by itself and
+// reports CHASE_FLUSH, CHASE_CONVERGED or CHASE_MAXITER in ChaseState.
+#include "symeig_common.cuh"
+
+namespace symeig {
+
+namespace {
+
+__device__ __forceinline__ double jl_max(double a, double b) { return (a > b || a != a) ? a : b; }
+
+// LinearAlgebra.givensAlgorithm (LAPACK 3.2 DLARTG port), as called by get_rotation.
+__device__ __forceinline__ void givens(double f, double g, double& cs, double& sn, double& r)
+{
+    const double safmn2 = 0x1p-485;
+    const double safmx2 = 0x1p+485;
+    if (g == 0.0) {
+        cs = 1.0; sn = 0.0; r = f;
+    } else if (f == 0.0) {
+        cs = 0.0; sn = 1.0; r = g;
+    } else {
+        double f1 = f, g1 = g;
+        double scale = jl_max(fabs(f1), fabs(g1));
+        if (scale >= safmx2) {
+            int count = 0;
+            do {
+                ++count;
+                f1 = __dmul_rn(f1, safmn2); g1 = __dmul_rn(g1, safmn2);
+                scale = jl_max(fabs(f1), fabs(g1));
+            } while (scale >= safmx2 && count < 20);
+            r = __dsqrt_rn(__dadd_rn(__dmul_rn(f1, f1), __dmul_rn(g1, g1)));
+            cs = __ddiv_rn(f1, r); sn = __ddiv_rn(g1, r);
+            for (int i = 0; i < count; ++i) r = __dmul_rn(r, safmx2);
+        } else if (scale <= safmn2) {
+            int count = 0;
+            do {
+                ++count;
+                f1 = __dmul_rn(f1, safmx2); g1 = __dmul_rn(g1, safmx2);
+                scale = jl_max(fabs(f1), fabs(g1));
+            } while (scale <= safmn2 && count < 64);  // 64 steps cover every subnormal
+            r = __dsqrt_rn(__dadd_rn(__dmul_rn(f1, f1), __dmul_rn(g1, g1)));
+            cs = __ddiv_rn(f1, r); sn = __ddiv_rn(g1, r);
+            for (int i = 0; i < count; ++i) r = __dmul_rn(r, safmn2);
+        } else {
+            r = __dsqrt_rn(__dadd_rn(__dmul_rn(f1, f1), __dmul_rn(g1, g1)));
+            cs = __ddiv_rn(f1, r); sn = __ddiv_rn(g1, r);
+        }
+        if (fabs(f) > fabs(g) && cs < 0.0) { cs = -cs; sn = -sn; r = -r; }
+    }
+}
+
+// is_offdiagonal_small(H, j, tol), 1-based j (src/bulge_chasing.jl:7-8).
+__device__ __forceinline__ bool is_small(const double* dv, const double* ev, int64_t j, double tol)
+{
+    return fabs(ev[j - 1]) <= __dmul_rn(tol, __dadd_rn(fabs(dv[j - 1]), fabs(dv[j])));
+}
+
+// Wilkinson shift from the trailing 2x2 block [a c; c b] (src/bulge_chasing.jl:239-265).
+__device__ __forceinline__ double wilkinson_shift(double a, double b, double c)
+{
+    const double scale = __dadd_rn(__dadd_rn(fabs(a), __dmul_rn(2.0, fabs(c))), fabs(b));
+    const double H11 = __ddiv_rn(a, scale), H12 = __ddiv_rn(c, scale), H22 = __ddiv_rn(b, scale);
+    const double t = __ddiv_rn(__dadd_rn(H11, H22), 2.0);
+    const double p = __dmul_rn(__dsub_rn(H11, t), __dsub_rn(H22, t));
+    const double q = __dmul_rn(H12, H12);
+    const double d = __dsub_rn(p, q);
+    const double sq = __dsqrt_rn(fabs(d));
+    const double l1 = __dadd_rn(t, sq), l2 = __dsub_rn(t, sq);
+    const double lam = fabs(__dsub_rn(H22, l1)) < fabs(__dsub_rn(H22, l2)) ? l1 : l2;
+    return __dmul_rn(lam, scale);
+}
+
+__device__ __forceinline__ double fsum(double u, double a, double v, double b)
+{
+    // u*a + v*b with the first product fused
+    return __fma_rn(u, a, __dmul_rn(v, b));
+}
+
+// Record (c,s) of rotation i (1-based).  thick[i] is the reference's layer_thickness (it
+// drives the capacity rule); place[i] is the grid layer used, equal to thick[i] in reference
+// mode (layer <= 0) or the sweep's common layer in exact-order mode.
+__device__ __forceinline__ void record(double* grid, int32_t* thick, int32_t* place, int64_t rows,
+                                       int64_t i, int32_t layer, double c, double s)
+{
+    const int32_t t = thick[i - 1] + 1;
+    thick[i - 1] = t;
+    if (layer <= 0) layer = t;
+    place[i - 1] = layer;
+    double* p = grid + 2 * ((i - 1) + (int64_t)(layer - 1) * rows);
+    p[0] = c;
+    p[1] = s;
+}
+
+// single_shift!(H, from, to, mu, givens, layer_thickness) (src/bulge_chasing.jl:11-144).
+// dv/ev are 0-based arrays; from/to 1-based.  Values the sweep itself produced travel in
+// registers; only untouched entries are loaded.
+__device__ void single_shift(double* __restrict__ dv, double* __restrict__ ev, int64_t from,
+                             int64_t to, double mu, double* __restrict__ grid,
+                             int32_t* __restrict__ thick, int32_t* __restrict__ place,
+                             int64_t rows, int32_t layer)
+{
+    const double H11 = dv[from - 1], H21 = ev[from - 1], H22 = dv[from];
+    double c, s, nrm;
+    givens(__dsub_rn(H11, mu), H21, c, s, nrm);
+    const double H11p = fsum(c, H11, s, H21);
+    const double H21p = __fma_rn(c, H21, -__dmul_rn(s, H11));
+    const double H12p = fsum(c, H21, s, H22);
+    const double H22p = __fma_rn(c, H22, -__dmul_rn(s, H21));
+    const double H11pp = fsum(H11p, c, H12p, s);
+    const double H12pp = __fma_rn(H12p, c, -__dmul_rn(H11p, s));
+    const double H22pp = __fma_rn(H22p, c, -__dmul_rn(H21p, s));
+    dv[from - 1] = H11pp;
+    dv[from] = H22pp;
+    ev[from - 1] = H12pp;
+    double bulge = 0.0;
+    double e_next = 0.0;  // ev[i] (1-based) entering step i
+    if (from + 2 <= to) {
+        const double H23 = ev[from];
+        bulge = __dmul_rn(s, H23);
+        e_next = __dmul_rn(c, H23);
+        ev[from] = e_next;
+    }
+    record(grid, thick, place, rows, from, layer, c, s);
+
+    double p1 = H12pp;      // ev[i-1] (1-based) entering step i
+    double B11 = H22pp;     // dv[i]   (1-based) entering step i
+    // untouched entries for the first loop step
+    double B22_n = (from + 1 <= to - 1) ? dv[from + 1] : 0.0;
+    double B23_n = (from + 3 <= to) ? ev[from + 1] : 0.0;
+    for (int64_t i = from + 1; i <= to - 1; ++i) {
+        const double B22 = B22_n, B23 = B23_n;
+        // prefetch for step i+1: dv[i+2], ev[i+2] (1-based)
+        if (i + 1 <= to - 1) B22_n = dv[i + 1];
+        if (i + 3 <= to) B23_n = ev[i + 1];
+        givens(p1, bulge, c, s, nrm);
+        ev[i - 2] = nrm;
+        const double B21 = e_next;
+        const double B11p = fsum(c, B11, s, B21);
+        const double B21p = __fma_rn(c, B21, -__dmul_rn(s, B11));
+        const double B12p = fsum(c, B21, s, B22);
+        const double B22p = __fma_rn(c, B22, -__dmul_rn(s, B21));
+        const double B11pp = fsum(B11p, c, B12p, s);
+        const double B12pp = __fma_rn(B12p, c, -__dmul_rn(B11p, s));
+        const double B22pp = __fma_rn(B22p, c, -__dmul_rn(B21p, s));
+        dv[i - 1] = B11pp;
+        dv[i] = B22pp;
+        ev[i - 1] = B12pp;
+        if (i + 2 <= to) {
+            bulge = __dmul_rn(s, B23);
+            e_next = __dmul_rn(c, B23);
+            ev[i] = e_next;
+        }
+        record(grid, thick, place, rows, i, layer, c, s);
+        p1 = B12pp;
+        B11 = B22pp;
+    }
+}
+
+__device__ __forceinline__ int32_t warp_max(int32_t v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// One flush: the reference's inner loop from `to = last_block_ends_at` until the matrix is
+// split into converged parts, every block has reached max_layers, or iter > maxiter.
+//
+// Exact-order placement (st->exact_order != 0).  The reference applies a flush's grid in
+// layer-major order, which equals the order the chase made the rotations only while every
+// sweep meets equal layer counts on its indices; when a split block re-merges it does not,
+// and the reference's Q loses accuracy.  In exact-order mode every rotation of a sweep over
+// [from, to] goes to the single layer
+//     L = 1 + max(place[from..to-1], place[to], place[from-1] - 1)
+// and skipped slots are set to (1,0), so the layer-major order of the grid is the chase's
+// order.  The chase itself (and so every eigenvalue) is the reference's.  A sweep whose layer
+// would exceed the grid's capacity ends the flush early (st->early_flushes counts these).
+__global__ void __launch_bounds__(32, 1)
+chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __restrict__ ev,
+             double* __restrict__ grid, int32_t* __restrict__ thick, int32_t* __restrict__ place)
+{
+    const int lane = threadIdx.x;
+    const int64_t n = st->n;
+    const int64_t start = st->start;
+    const double tol = st->tol;
+    const int32_t max_layers = st->max_layers;
+    const int32_t grid_layers = st->grid_layers;
+    const bool exact = st->exact_order != 0;
+    const int64_t maxiter = st->maxiter;
+    int64_t iter = st->iter;
+    int64_t lbe = st->last_block_ends_at;
+    const int64_t rows = n > 1 ? n - 1 : 1;
+
+    for (int64_t q = lane; q < n; q += 32) {
+        thick[q] = 0;
+        place[q] = 0;
+    }
+    __syncwarp();
+
+    bool did = false;
+    int64_t rotations = 0, min_from = n + 1, max_to = 0, early = 0;
+    int32_t status = CHASE_RUNNING;
+    int64_t to = lbe;
+
+    for (;;) {
+        if (iter > maxiter) { status = CHASE_MAXITER; break; }
+        if (to <= start) break;
+        // from = largest j+1 with is_small(j), j in [start, to-1]; start if none
+        int64_t from = start;
+        for (int64_t base = to - 1; base >= start; base -= 32) {
+            const int64_t j = base - lane;
+            const bool sm = (j >= start) && is_small(dv, ev, j, tol);
+            const unsigned mask = __ballot_sync(0xffffffffu, sm);
+            if (mask) { from = base - (__ffs(mask) - 1) + 1; break; }
+        }
+        if (from == to) {
+            if (lane == 0) ev[from - 2] = 0.0;
+            if (to == lbe) lbe -= 1;
+            to -= 1;
+        } else {
+            int32_t mx = 0;
+            for (int64_t q = from - 1 + lane; q <= to - 1; q += 32) mx = max(mx, thick[q]);
+            mx = warp_max(mx);
+            if (mx == max_layers) {
+                to = from - 1;
+            } else {
+                int32_t layer = 0;
+                if (exact) {
+                    int32_t L = 0;
+                    for (int64_t q = from - 1 + lane; q <= to - 2; q += 32) L = max(L, place[q]);
+                    L = warp_max(L);
+                    if (to <= n - 1) L = max(L, place[to - 1]);
+                    if (from >= 2) L = max(L, place[from - 2] - 1);
+                    layer = L + 1;
+                    if (layer > grid_layers) { early = 1; break; }
+                    // slots skipped by the jump to `layer` hold the identity
+                    for (int64_t q = from - 1 + lane; q <= to - 2; q += 32)
+                        for (int32_t g = place[q] + 1; g < layer; ++g) {
+                            double* p = grid + 2 * (q + (int64_t)(g - 1) * rows);
+                            p[0] = 1.0;
+                            p[1] = 0.0;
+                        }
+                    __syncwarp();
+                }
+                if (lane == 0) {
+                    const double mu = wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
+                    single_shift(dv, ev, from, to, mu, grid, thick, place, rows, layer);
+                }
+                did = true;
+                iter += 1;
+                rotations += to - from;
+                min_from = min(min_from, from);
+                max_to = max(max_to, to);
+            }
+        }
+        __syncwarp();
+        if (to <= start) break;
+    }
+    __syncwarp();
+
+    int32_t kmax = 0;
+    for (int64_t q = lane; q < n; q += 32) kmax = max(kmax, place[q]);
+    kmax = warp_max(kmax);
+
+    if (lane == 0) {
+        if (status == CHASE_RUNNING) status = did ? CHASE_FLUSH : CHASE_CONVERGED;
+        st->status = status;
+        st->iter = iter;
+        st->last_block_ends_at = lbe;
+        st->rotations = rotations;
+        st->min_from = min_from;
+        st->max_to = max_to;
+        st->max_thickness = kmax;
+        st->total_rotations += rotations;
+        st->early_flushes += early;
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
+                         int32_t* place, cudaStream_t stream)
+{
+    chase_kernel<<<1, 32, 0, stream>>>(state, d, e, grid, thick, place);
+    return cudaGetLastError();
+}
+
+}  // namespace symeig

@@ -1,0 +1,92 @@
+// symeig_common.cuh -- shared definitions of the libsymeig.so kernels (sm_103a).
+//
+// Floating-point forms are fixed with the _rn intrinsics so nvcc cannot contract or
+// reassociate them; the CPU oracle uses the same forms, which lets the tests compare
+// device and oracle results bit for bit:
+//   rotation of a pair (x, y):   x' = fma(c, x, s*y);   y' = fma(c, y, -(s*x))
+// This is rmul!(A, G::Rotation2) of the reference (src/simple_givens.jl:53-65) with the
+// first product of each line fused.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace symeig {
+
+template <typename T> struct Pair;
+template <> struct Pair<double> { using type = double2; };
+template <> struct Pair<float>  { using type = float2; };
+
+__device__ __forceinline__ void rot(double& x, double& y, double c, double s)
+{
+    const double sy = __dmul_rn(s, y);
+    const double sx = __dmul_rn(s, x);
+    x = __fma_rn(c, x, sy);
+    y = __fma_rn(c, y, -sx);
+}
+
+__device__ __forceinline__ void rot(float& x, float& y, float c, float s)
+{
+    const float sy = __fmul_rn(s, y);
+    const float sx = __fmul_rn(s, x);
+    x = __fmaf_rn(c, x, sy);
+    y = __fmaf_rn(c, y, -sx);
+}
+
+// ---- chase state shared by the chase kernel and the host driver -------------------------
+enum ChaseStatus : int32_t {
+    CHASE_RUNNING   = 0,
+    CHASE_CONVERGED = 1,   // the flush recorded no rotation: the reference's `!did_a_thing && break`
+    CHASE_MAXITER   = 2,   // iter > maxiter: the reference returns (H, false, iter)
+    CHASE_FLUSH     = 3,   // rotations recorded; apply them, then chase again
+};
+
+struct ChaseState {
+    int64_t n;
+    int64_t start;               // always 1 (the reference's `start`)
+    int64_t last_block_ends_at;  // 1-based, as in the reference
+    int64_t iter;
+    int64_t maxiter;
+    double  tol;
+    int32_t max_layers;
+    int32_t grid_layers;         // layer capacity of the grid buffer
+    int32_t exact_order;         // 1: exact-order placement, 0: the reference's placement
+    int32_t status;
+    // outputs of the last flush
+    int64_t rotations;           // rotations recorded by the flush
+    int64_t min_from;            // 1-based smallest `from` of any sweep
+    int64_t max_to;              // 1-based largest `to` of any sweep
+    int64_t max_thickness;       // thickest column of the rotation grid (placement layers)
+    int64_t total_rotations;
+    int64_t early_flushes;       // flushes ended because a sweep's layer exceeded grid_layers
+};
+
+// ---- launch helpers (defined in the .cu files) ------------------------------------------
+// Apply geometry of one pass of the wave-window kernel: columns [c0, c0 + n_loc) of Q and
+// layers [L0, L0 + layers) of the (n-1) x * rotation grid.
+struct ApplyPass {
+    int64_t c0, n_loc, L0, layers;
+};
+
+// Layers one pass of the wave-window kernel handles for element type T.
+template <typename T> int64_t apply_layers_per_pass();
+
+// Bytes of the wave table one pass needs.
+template <typename T> size_t apply_table_bytes(int64_t n_loc, int64_t layers);
+
+// Build the wave table of one pass from a grid of (c,s) pairs in Julia layout
+// (grid_rows rows, column L = layer L).  When place != nullptr, layer L of rotation i is
+// the identity unless L < place[i] (the qr flush: the reference fills unused slots with
+// (1,0); here the chase writes only slots below place[i]).  Then run the wave-window
+// kernel on Q.
+// ev_begin/ev_end (may be null) are recorded on `stream` around the wave kernel alone.
+template <typename Tsrc, typename T>
+cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t grid_rows,
+                       const int32_t* thick, const ApplyPass& pass, void* table,
+                       cudaStream_t stream, cudaEvent_t ev_begin = nullptr,
+                       cudaEvent_t ev_end = nullptr);
+
+cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
+                         int32_t* place, cudaStream_t stream);
+
+}  // namespace symeig
