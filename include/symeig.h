@@ -127,6 +127,23 @@ int symeig_apply_givens_f64_dev(symeig_handle h, double* A, int64_t lda, int64_t
 int symeig_apply_givens_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t m, int64_t n,
                                 const float* cs, int64_t k);
 
+/* ---- bulk apply without any allocation -------------------------------------------------- *
+ * No counterpart in the reference.  For callers that cannot allocate device memory at call
+ * time (their device memory belongs to another allocator that reserved it up front, or
+ * cudaMalloc's implicit synchronisation is unacceptable on their path).  Same operation and
+ * arguments as symeig_apply_givens_f64_dev, but it needs no handle: A and cs are device
+ * pointers, `stream` is a cudaStream_t (NULL = legacy default stream) on the current device,
+ * and the call is asynchronous.  Its wave table lives in a file-scope device array of
+ * SYMEIG_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit; n must
+ * satisfy (n + 71) * 1024 <= SYMEIG_NOALLOC_SCRATCH_BYTES (n <= 32697), else
+ * SYMEIG_ERR_SIZE is returned and nothing runs.  The first call on a device resolves the
+ * array's address (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the array: calls whose kernels overlap on the
+ * GPU race; calls on one stream are ordered and safe. */
+#define SYMEIG_NOALLOC_SCRATCH_BYTES (32u << 20)
+int symeig_apply_givens_f64_noalloc(double* A, int64_t lda, int64_t m, int64_t n,
+                                    const double* cs, int64_t k, void* stream);
+
 /* ---- eigen_decomp!  (src/bulge_chasing.jl:290-299) ----------------------------------- *
  * Q (n x n, ldq >= n) is set to the identity, then qr_algorithm! runs with the default
  * max_layers = 128, tol = eps, maxiter = 100n.  d/e overwritten as in symeig_qr_f64. */

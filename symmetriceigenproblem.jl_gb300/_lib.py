@@ -44,6 +44,7 @@ SIGNATURES = {
     "symeig_apply_givens_f32": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
     "symeig_apply_givens_f64_dev": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
     "symeig_apply_givens_f32_dev": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
+    "symeig_apply_givens_f64_noalloc": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp]),
     "symeig_eigen_decomp_f64": (ctypes.c_int, [c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, P_i32, P_i64]),
 }
 
