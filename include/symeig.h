@@ -50,6 +50,7 @@ typedef struct {
     int64_t early_flushes;   /* flushes ended early to keep exact rotation order (see below)  */
     int64_t wave_launches;   /* launches of the wave-window Givens kernel                 */
     double  wave_kernel_ms;  /* their summed device time (only with kernel timing on)     */
+    int64_t device_errors;   /* nonzero if a kernel's bounded wait gave up (sticky)        */
 } symeig_stats;
 
 /* Create a handle bound to CUDA device `device`.  Replaces nothing in the reference (the
@@ -127,6 +128,31 @@ int symeig_apply_givens_f64_dev(symeig_handle h, double* A, int64_t lda, int64_t
 int symeig_apply_givens_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t m, int64_t n,
                                 const float* cs, int64_t k);
 
+/* ---- batched qr_algorithm! ---------------------------------------------------------------- *
+ * count independent solves, each exactly qr_algorithm!(SymTridiagonal(d_i, e_i), Q_i,
+ * max_layers, tol, maxiter_factor * n_i) (src/bulge_chasing.jl:146; maxiter_factor <= 0
+ * means the reference's 100).  Packed layout: matrix i has order n[i]; its diagonal is
+ * d[sum_{j<i} n_j ...], its off-diagonal e[sum_{j<i} (n_j - 1) ...], its Q (n_i x n_i,
+ * column-major, leading dimension n_i, overwritten with Q_i * prod(G)) at
+ * Q[sum_{j<i} n_j^2 ...]; Q may be NULL (eigenvalues only).  n, converged and iters are host
+ * arrays of count entries.  The reference has no batched entry point; this replaces a loop of
+ * qr_algorithm! calls.  Matrices run one flush per round: a one-lane-per-matrix chase, then
+ * a persistent wave-kernel launch over a device-built queue of (matrix, row tile) items; one
+ * round is captured as a CUDA graph and replayed until every matrix has finished. */
+int symeig_qr_batched_f64(symeig_handle h, int64_t count, const int64_t* n, double* d, double* e,
+                          double* Q, int32_t max_layers, double tol, int64_t maxiter_factor,
+                          int32_t* converged, int64_t* iters);
+int symeig_qr_batched_f64_dev(symeig_handle h, int64_t count, const int64_t* n, double* d,
+                              double* e, double* Q, int32_t max_layers, double tol,
+                              int64_t maxiter_factor, int32_t* converged, int64_t* iters);
+/* Autotuner of the batched apply: times each candidate tile shape (0: 16 rows x 8 layer
+ * groups of 8; 1: 32 rows x 4 groups of 16 -- both 64 layers per pass) on a synthetic batch
+ * of each size class (n <= split, n > split) and keeps the faster one per class, process-wide.
+ * ms (may be NULL) receives 4 timings [class][shape].  No reference counterpart. */
+int symeig_batched_autotune(symeig_handle h, double* ms);
+/* Read (set = 0) or write (set != 0) the batched tuning: class split and shape per class. */
+int symeig_batched_tuning(int64_t* split, int32_t* shape_small, int32_t* shape_large, int32_t set);
+
 /* ---- bulk apply without any allocation -------------------------------------------------- *
  * No counterpart in the reference.  For callers that cannot allocate device memory at call
  * time (their device memory belongs to another allocator that reserved it up front, or
@@ -135,7 +161,7 @@ int symeig_apply_givens_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t 
  * pointers, `stream` is a cudaStream_t (NULL = legacy default stream) on the current device,
  * and the call is asynchronous.  Its wave table lives in a file-scope device array of
  * SYMEIG_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until exit; n must
- * satisfy (n + 71) * 1024 <= SYMEIG_NOALLOC_SCRATCH_BYTES (n <= 32697), else
+ * satisfy ceil((n + 71) / 9) * 10368 <= SYMEIG_NOALLOC_SCRATCH_BYTES (n <= 29053), else
  * SYMEIG_ERR_SIZE is returned and nothing runs.  The first call on a device resolves the
  * array's address (cudaGetSymbolAddress) with that device current; make that first call
  * before any stream capture.  All calls share the array: calls whose kernels overlap on the

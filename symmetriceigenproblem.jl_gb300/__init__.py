@@ -9,6 +9,8 @@ from .api import (  # noqa: F401
     SymTridiagonal,
     bulk_wave_order_2x2_rmul_,
     bulk_wave_order_2x2_rmul_parallel_,
+    batched_autotune,
+    qr_algorithm_batched_,
     eigen_decomp_,
     givens_buffer,
     qr_algorithm_,

@@ -45,6 +45,10 @@ SIGNATURES = {
     "symeig_apply_givens_f64_dev": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
     "symeig_apply_givens_f32_dev": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
     "symeig_apply_givens_f64_noalloc": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp]),
+    "symeig_qr_batched_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_dbl, c_i64, c_vp, c_vp]),
+    "symeig_qr_batched_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_dbl, c_i64, c_vp, c_vp]),
+    "symeig_batched_autotune": (ctypes.c_int, [c_vp, c_vp]),
+    "symeig_batched_tuning": (ctypes.c_int, [P_i64, P_i32, P_i32, c_i32]),
     "symeig_eigen_decomp_f64": (ctypes.c_int, [c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, P_i32, P_i64]),
 }
 
@@ -53,7 +57,7 @@ class Stats(ctypes.Structure):
     _fields_ = [("iterations", c_i64), ("flushes", c_i64), ("rotations", c_i64),
                 ("applied_rotation_rows", c_i64), ("chase_ms", c_dbl), ("apply_ms", c_dbl),
                 ("total_ms", c_dbl), ("early_flushes", c_i64), ("wave_launches", c_i64),
-                ("wave_kernel_ms", c_dbl)]
+                ("wave_kernel_ms", c_dbl), ("device_errors", c_i64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

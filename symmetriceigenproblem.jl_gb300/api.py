@@ -206,3 +206,58 @@ def eigen_decomp_(H: SymTridiagonal, handle: Handle | None = None):
         Q = np.asfortranarray(np.eye(n))
     _, converged, iters = qr_algorithm_(H, Q, handle=handle)
     return H.dv, Q
+
+
+def qr_algorithm_batched_(d, e, n, Q=None, max_layers: int = 128, tol: float | None = None,
+                          maxiter_factor: int = 100, handle: Handle | None = None):
+    """Batched qr_algorithm!: count independent solves in one call (no reference counterpart;
+    it replaces a loop of qr_algorithm! calls, src/bulge_chasing.jl:146).
+
+    d, e, Q are packed: matrix i has order n[i], its diagonal/off-diagonal follow the previous
+    matrices' in d (sum n) and e (sum n-1), and its Q (n_i x n_i column-major) follows the
+    previous ones in Q (sum n^2, flat).  All three are numpy arrays (host) or CUDA torch
+    tensors (device); Q may be None (eigenvalues only).  Returns (converged, iters) numpy
+    arrays of length count."""
+    n = np.ascontiguousarray(np.asarray(n, dtype=np.int64))
+    count = int(n.shape[0])
+    conv = np.zeros(count, dtype=np.int32)
+    iters = np.zeros(count, dtype=np.int64)
+    tol = EPS64 if tol is None else float(tol)
+    dev = _is_torch(d)
+    arrays = (d, e) + ((Q,) if Q is not None else ())
+    for a in arrays:
+        if dev:
+            if not (_is_torch(a) and a.is_cuda and a.dtype == torch.float64 and a.is_contiguous()):
+                raise TypeError("d, e, Q must all be contiguous CUDA float64 tensors")
+        else:
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous and a.flags.writeable):
+                raise TypeError("d, e, Q must all be writeable contiguous float64 numpy arrays")
+    if int(d.shape[0]) != int(n.sum()) or int(e.shape[0]) != int((n - 1).sum()):
+        raise ValueError("packed d / e sizes do not match n")
+    if Q is not None and int(Q.numel() if dev else Q.size) != int((n * n).sum()):
+        raise ValueError("packed Q size does not match n")
+    ptr = (lambda a: a.data_ptr()) if dev else (lambda a: a.ctypes.data)
+    h = handle or default_handle(d.device.index if dev else 0)
+    args = (count, ctypes.c_void_p(n.ctypes.data), ctypes.c_void_p(ptr(d)),
+            ctypes.c_void_p(ptr(e) if int(e.shape[0]) else None),
+            ctypes.c_void_p(ptr(Q) if Q is not None else None), int(max_layers), tol,
+            int(maxiter_factor), ctypes.c_void_p(conv.ctypes.data), ctypes.c_void_p(iters.ctypes.data))
+    if dev:
+        with h.on_stream(torch.cuda.current_stream(d.device).cuda_stream):
+            h.call("symeig_qr_batched_f64_dev", *args)
+    else:
+        if int(e.shape[0]) == 0:
+            ebuf = np.zeros(1)
+            args = args[:3] + (ctypes.c_void_p(ebuf.ctypes.data),) + args[4:]
+        h.call("symeig_qr_batched_f64", *args)
+    return conv.astype(bool), iters
+
+
+def batched_autotune(handle: Handle | None = None):
+    """Run the batched-apply autotuner; returns ({class: shape}, timings ms [class][shape])."""
+    h = handle or default_handle(0)
+    ms = (ctypes.c_double * 4)()
+    h.call("symeig_batched_autotune", ms)
+    split, s0, s1 = c_i64(), c_i32(), c_i32()
+    h._lib.symeig_batched_tuning(ctypes.byref(split), ctypes.byref(s0), ctypes.byref(s1), 0)
+    return {"split": split.value, "shape_small": s0.value, "shape_large": s1.value}, [list(ms[0:2]), list(ms[2:4])]

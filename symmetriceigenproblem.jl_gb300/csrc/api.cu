@@ -54,6 +54,7 @@ struct symeig_context {
     cudaEvent_t ev_consumed[2] = {nullptr, nullptr};
     cudaEvent_t ev_main = nullptr;
     DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs;
+    int* derr = nullptr;   // device error word of the wave kernels (bounded waits)
     int32_t exact_order = 1;  // rotation placement of the qr driver
     ChaseState* h_state = nullptr;  // pinned
     std::vector<cudaEvent_t> timing;  // pool of timing events
@@ -94,7 +95,8 @@ bool mul_overflows(int64_t a, int64_t b)
 
 int validate_matrix(const void* A, int64_t lda, int64_t m, int64_t n)
 {
-    if (m < 0 || n < 0) return SYMEIG_ERR_SIZE;
+    // the kernels index columns with 32-bit integers
+    if (m < 0 || n < 0 || n > (int64_t)1 << 30) return SYMEIG_ERR_SIZE;
     if (m > 0 && n > 0 && !A) return SYMEIG_ERR_NULL;
     if (m > 0 && lda < m) return SYMEIG_ERR_LD;
     if (mul_overflows(lda, n)) return SYMEIG_ERR_SIZE;
@@ -146,7 +148,8 @@ int apply_grid(symeig_handle h, T* Q, int64_t ldq, int64_t m, const Tsrc* grid, 
             if (!e0 || !e1) return SYMEIG_ERR_CUDA;
             h->kpending = true;
         }
-        CK((apply_pass<Tsrc, T>(Q, ldq, m, grid, grid_rows, thick, pass, h->table.ptr, s, e0, e1)));
+        CK((apply_pass<Tsrc, T>(Q, ldq, m, grid, grid_rows, thick, pass, h->table.ptr, h->derr, s,
+                                e0, e1)));
         h->stats.wave_launches += 1;
     }
     h->stats.applied_rotation_rows += (n_loc - 1) * layers * m;
@@ -377,6 +380,8 @@ int symeig_create(symeig_handle* out, int device)
     }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&h->ev_main, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMallocHost((void**)&h->h_state, sizeof(ChaseState));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->derr, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(h->derr, 0, sizeof(int));
     if (e != cudaSuccess) {
         symeig_destroy(h);
         return cuda_status(e);
@@ -406,6 +411,7 @@ int symeig_destroy(symeig_handle h)
     for (cudaEvent_t ev : h->timing) cudaEventDestroy(ev);
     for (cudaEvent_t ev : h->kpool) cudaEventDestroy(ev);
     if (h->h_state) cudaFreeHost(h->h_state);
+    if (h->derr) cudaFree(h->derr);
     if (h->chase_stream) cudaStreamDestroy(h->chase_stream);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
@@ -459,6 +465,9 @@ int symeig_get_stats(symeig_handle h, symeig_stats* out)
         h->stats.wave_kernel_ms = ms;
         h->kpending = false;
     }
+    int derr = 0;
+    CK(cudaMemcpy(&derr, h->derr, sizeof(int), cudaMemcpyDeviceToHost));
+    h->stats.device_errors = derr;
     *out = h->stats;
     return SYMEIG_OK;
 }
@@ -539,6 +548,86 @@ int symeig_apply_givens_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t 
                                 const float* cs, int64_t k)
 {
     return apply_dev<float>(h, A, lda, m, n, cs, k);
+}
+
+int symeig_qr_batched_f64_dev(symeig_handle h, int64_t count, const int64_t* n, double* d,
+                              double* e, double* Q, int32_t max_layers, double tol,
+                              int64_t maxiter_factor, int32_t* converged, int64_t* iters)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (count < 0) return SYMEIG_ERR_SIZE;
+    if (count > 0 && (!n || !d || !e)) return SYMEIG_ERR_NULL;
+    if (max_layers < 1) return SYMEIG_ERR_LAYERS;
+    begin_call(h);
+    auto t0 = std::chrono::steady_clock::now();
+    // The rounds are captured as a CUDA graph, which needs a capturable stream (not the legacy
+    // default stream): run on the handle's own stream, ordered after the caller's stream.
+    CK(cudaEventRecord(h->ev_main, h->stream));
+    CK(cudaStreamWaitEvent(h->own_stream, h->ev_main, 0));
+    rc = qr_batched_dev(h->device, h->own_stream, count, n, d, e, Q, max_layers, tol, maxiter_factor,
+                        h->exact_order, converged, iters, &h->stats.flushes, nullptr);
+    for (int64_t i = 0; i < count && iters; ++i) h->stats.iterations += iters[i];
+    h->stats.total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int symeig_qr_batched_f64(symeig_handle h, int64_t count, const int64_t* n, double* d, double* e,
+                          double* Q, int32_t max_layers, double tol, int64_t maxiter_factor,
+                          int32_t* converged, int64_t* iters)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (count < 0) return SYMEIG_ERR_SIZE;
+    if (count == 0) return SYMEIG_OK;
+    if (!n || !d || !e) return SYMEIG_ERR_NULL;
+    int64_t nd = 0, ne = 0, nq = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        if (n[i] < 1) return SYMEIG_ERR_SIZE;
+        nd += n[i];
+        ne += n[i] - 1;
+        nq += n[i] * n[i];
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = h->stream;
+    CK(h->d.ensure(nd * sizeof(double)));
+    CK(h->e.ensure(std::max<int64_t>(ne, 1) * sizeof(double)));
+    if (Q) CK(h->q.ensure(nq * sizeof(double)));
+    CK(cudaMemcpyAsync(h->d.ptr, d, nd * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (ne) CK(cudaMemcpyAsync(h->e.ptr, e, ne * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (Q) CK(cudaMemcpyAsync(h->q.ptr, Q, nq * sizeof(double), cudaMemcpyHostToDevice, s));
+    rc = symeig_qr_batched_f64_dev(h, count, n, (double*)h->d.ptr, (double*)h->e.ptr,
+                                   Q ? (double*)h->q.ptr : nullptr, max_layers, tol,
+                                   maxiter_factor, converged, iters);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(d, h->d.ptr, nd * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (ne) CK(cudaMemcpyAsync(e, h->e.ptr, ne * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (Q) CK(cudaMemcpyAsync(Q, h->q.ptr, nq * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    h->stats.total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return SYMEIG_OK;
+}
+
+int symeig_batched_autotune(symeig_handle h, double* ms)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return batched_autotune(h->device, h->stream, ms);
+}
+
+int symeig_batched_tuning(int64_t* split, int32_t* shape_small, int32_t* shape_large, int32_t set)
+{
+    if (!split || !shape_small || !shape_large) return SYMEIG_ERR_NULL;
+    if (set) {
+        if (*split < 1 || *shape_small < 0 || *shape_small > 1 || *shape_large < 0 || *shape_large > 1)
+            return SYMEIG_ERR_SIZE;
+        batched_set_tuning(*split, *shape_small, *shape_large);
+    } else {
+        batched_get_tuning(split, shape_small, shape_large);
+    }
+    return SYMEIG_OK;
 }
 
 int symeig_eigen_decomp_f64(symeig_handle h, double* d, double* e, int64_t n, double* Q,

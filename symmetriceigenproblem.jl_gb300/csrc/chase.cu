@@ -293,12 +293,126 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
     }
 }
 
+
+// ---- batched chase: one lane per matrix --------------------------------------------------
+//
+// A chase step is a chain of ~55 dependent FP64 operations, and on GB300 an FP64 instruction
+// occupies its sub-partition's FP64 unit for 64 cycles whether 1 or 32 lanes are active.  So
+// for many independent matrices each lane runs its own matrix's flush: 32 chases share every
+// FP64 instruction.  The host sorts matrices by size so that a warp's lanes sweep similar
+// lengths.  The scans (deflation, thickest column, exact-order layer) are serial per lane.
+
+// One flush of one matrix (the same steps, in the same order, as chase_kernel).
+__device__ void chase_flush_lane(ChaseState* __restrict__ st, double* __restrict__ dv,
+                                 double* __restrict__ ev, double* __restrict__ grid,
+                                 int32_t* __restrict__ thick, int32_t* __restrict__ place)
+{
+    const int64_t n = st->n;
+    const int64_t start = st->start;
+    const double tol = st->tol;
+    const int32_t max_layers = st->max_layers;
+    const int32_t grid_layers = st->grid_layers;
+    const bool exact = st->exact_order != 0;
+    const int64_t maxiter = st->maxiter;
+    int64_t iter = st->iter;
+    int64_t lbe = st->last_block_ends_at;
+    const int64_t rows = n > 1 ? n - 1 : 1;
+
+    for (int64_t q = 0; q < n; ++q) {
+        thick[q] = 0;
+        place[q] = 0;
+    }
+    bool did = false;
+    int64_t rotations = 0, min_from = n + 1, max_to = 0, early = 0;
+    int32_t status = CHASE_RUNNING;
+    int64_t to = lbe;
+    for (;;) {
+        if (iter > maxiter) { status = CHASE_MAXITER; break; }
+        if (to <= start) break;
+        int64_t from = to;
+        while (from > start && !is_small(dv, ev, from - 1, tol)) from -= 1;
+        if (from == to) {
+            ev[from - 2] = 0.0;
+            if (to == lbe) lbe -= 1;
+            to -= 1;
+        } else {
+            int32_t mx = 0;
+            for (int64_t q = from - 1; q <= to - 1; ++q) mx = max(mx, thick[q]);
+            if (mx == max_layers) {
+                to = from - 1;
+            } else {
+                int32_t layer = 0;
+                if (exact) {
+                    int32_t L = 0;
+                    for (int64_t q = from - 1; q <= to - 2; ++q) L = max(L, place[q]);
+                    if (to <= n - 1) L = max(L, place[to - 1]);
+                    if (from >= 2) L = max(L, place[from - 2] - 1);
+                    layer = L + 1;
+                    if (layer > grid_layers) { early = 1; break; }
+                    for (int64_t q = from - 1; q <= to - 2; ++q)
+                        for (int32_t g = place[q] + 1; g < layer; ++g) {
+                            double* p = grid + 2 * (q + (int64_t)(g - 1) * rows);
+                            p[0] = 1.0;
+                            p[1] = 0.0;
+                        }
+                }
+                const double mu = wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
+                single_shift(dv, ev, from, to, mu, grid, thick, place, rows, layer);
+                did = true;
+                iter += 1;
+                rotations += to - from;
+                min_from = min(min_from, from);
+                max_to = max(max_to, to);
+            }
+        }
+        if (to <= start) break;
+    }
+    int32_t kmax = 0;
+    for (int64_t q = 0; q < n; ++q) kmax = max(kmax, place[q]);
+    if (status == CHASE_RUNNING) status = did ? CHASE_FLUSH : CHASE_CONVERGED;
+    st->status = status;
+    st->iter = iter;
+    st->last_block_ends_at = lbe;
+    st->rotations = rotations;
+    st->min_from = min_from;
+    st->max_to = max_to;
+    st->max_thickness = kmax;
+    st->total_rotations += rotations;
+    st->early_flushes += early;
+}
+
+__global__ void __launch_bounds__(32)
+chase_batched_kernel(const BatchMat* __restrict__ mats, const int32_t* __restrict__ order,
+                     int32_t count, ChaseState* __restrict__ states, double* __restrict__ d,
+                     double* __restrict__ e, double* __restrict__ grids,
+                     int32_t* __restrict__ thick, int32_t* __restrict__ place)
+{
+    const int32_t k = blockIdx.x * 32 + threadIdx.x;
+    if (k >= count) return;
+    const int32_t i = order[k];
+    ChaseState* st = states + i;
+    const int32_t s0 = st->status;
+    if (s0 == CHASE_CONVERGED || s0 == CHASE_MAXITER) return;
+    const BatchMat mt = mats[i];
+    chase_flush_lane(st, d + mt.doff, e + mt.eoff, grids + mt.goff, thick + mt.doff, place + mt.doff);
+}
+
 }  // namespace
 
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
                          int32_t* place, cudaStream_t stream)
 {
     chase_kernel<<<1, 32, 0, stream>>>(state, d, e, grid, thick, place);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_chase_batched(const BatchMat* mats, const int32_t* order, int32_t count,
+                                 ChaseState* states, double* d, double* e, double* grids,
+                                 int32_t* thick, int32_t* place, cudaStream_t stream)
+{
+    if (count <= 0) return cudaSuccess;
+    chase_batched_kernel<<<(count + 31) / 32, 32, 0, stream>>>(mats, order, count, states, d, e,
+                                                               grids, thick, place);
     return cudaGetLastError();
 }
 

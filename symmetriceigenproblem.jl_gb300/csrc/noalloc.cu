@@ -24,26 +24,33 @@
 namespace symeig {
 namespace {
 
-// The scratch: one pass's wave table (sized for n + 71 waves x 64 (c,s) pairs of FP64).
+// The scratch: one pass's wave table, and the kernel's error word (set to 1 if a bounded
+// wait inside the kernel gave up; never cleared by the library).
 static __device__ __align__(256) unsigned char g_noalloc_table[SYMEIG_NOALLOC_SCRATCH_BYTES];
+static __device__ int g_noalloc_err;
 
 constexpr int kMaxDevices = 64;
 std::mutex g_setup_lock;
 void* g_table_addr[kMaxDevices] = {};  // device address of g_noalloc_table, per device
+void* g_err_addr[kMaxDevices] = {};    // device address of g_noalloc_err, per device
 
-// Once per device, with that device current: resolve the device address of the array.  In
-// host code `g_noalloc_table` names a host-side stand-in, never a device address.
-int table_address(void** out)
+// Once per device, with that device current: resolve the device addresses of the arrays.
+// In host code `g_noalloc_table` names a host-side stand-in, never a device address.
+int table_address(void** table, int** err)
 {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return SYMEIG_ERR_CUDA;
     std::lock_guard<std::mutex> lk(g_setup_lock);
     if (!g_table_addr[dev]) {
         void* p = nullptr;
+        void* q = nullptr;
         if (cudaGetSymbolAddress(&p, g_noalloc_table) != cudaSuccess || !p) return SYMEIG_ERR_CUDA;
+        if (cudaGetSymbolAddress(&q, g_noalloc_err) != cudaSuccess || !q) return SYMEIG_ERR_CUDA;
         g_table_addr[dev] = p;
+        g_err_addr[dev] = q;
     }
-    *out = g_table_addr[dev];
+    *table = g_table_addr[dev];
+    *err = (int*)g_err_addr[dev];
     return SYMEIG_OK;
 }
 
@@ -54,7 +61,7 @@ extern "C" int symeig_apply_givens_f64_noalloc(double* A, int64_t lda, int64_t m
                                                const double* cs, int64_t k, void* stream)
 {
     using namespace symeig;
-    if (m < 0 || n < 0 || k < 0) return SYMEIG_ERR_SIZE;
+    if (m < 0 || n < 0 || k < 0 || n > (int64_t)1 << 30) return SYMEIG_ERR_SIZE;
     if (m > 0 && n > 0 && !A) return SYMEIG_ERR_NULL;
     if (m > 0 && lda < m) return SYMEIG_ERR_LD;
     if (m == 0 || n < 2 || k == 0) return SYMEIG_OK;
@@ -62,12 +69,13 @@ extern "C" int symeig_apply_givens_f64_noalloc(double* A, int64_t lda, int64_t m
     const int64_t per = apply_layers_per_pass<double>();
     if (apply_table_bytes<double>(n, per) > (size_t)SYMEIG_NOALLOC_SCRATCH_BYTES) return SYMEIG_ERR_SIZE;
     void* table = nullptr;
-    int rc = table_address(&table);
+    int* err = nullptr;
+    int rc = table_address(&table, &err);
     if (rc) return rc;
     cudaStream_t s = (cudaStream_t)stream;
     for (int64_t L0 = 0; L0 < k; L0 += per) {
         ApplyPass pass{0, n, L0, k - L0 < per ? k - L0 : per};
-        if (apply_pass<double, double>(A, lda, m, cs, n - 1, nullptr, pass, table, s) != cudaSuccess)
+        if (apply_pass<double, double>(A, lda, m, cs, n - 1, nullptr, pass, table, err, s) != cudaSuccess)
             return SYMEIG_ERR_CUDA;
     }
     return SYMEIG_OK;

@@ -25,6 +25,19 @@ __device__ __forceinline__ void rot(double& x, double& y, double c, double s)
     y = __fma_rn(c, y, -sx);
 }
 
+// The same rotation with the two products issued as FMAs with a -0.0 addend.  For every
+// product p (including +-0, +-inf and NaN), p + (-0.0) == p bit for bit, so
+// fma(s, y, -0.0) == s*y exactly; on GB300 an FP64 FMA issues at ~1.18x the rate of an FP64
+// multiply (measured), and a rotation is half multiplies.  `nz` must be -0.0 supplied at run
+// time (a kernel argument), so that no compiler pass folds the FMA back into a multiply.
+__device__ __forceinline__ void rot_fma(double& x, double& y, double c, double s, double nz)
+{
+    const double sy = __fma_rn(s, y, nz);
+    const double sx = __fma_rn(s, x, nz);
+    x = __fma_rn(c, x, sy);
+    y = __fma_rn(c, y, -sx);
+}
+
 __device__ __forceinline__ void rot(float& x, float& y, float c, float s)
 {
     const float sy = __fmul_rn(s, y);
@@ -79,14 +92,41 @@ template <typename T> size_t apply_table_bytes(int64_t n_loc, int64_t layers);
 // the identity unless L < place[i] (the qr flush: the reference fills unused slots with
 // (1,0); here the chase writes only slots below place[i]).  Then run the wave-window
 // kernel on Q.
-// ev_begin/ev_end (may be null) are recorded on `stream` around the wave kernel alone.
+// `err` is a device word the kernel sets to 1 if a bounded wait gave up (it never waits on
+// anything but its own bulk copies).  ev_begin/ev_end (may be null) are recorded on
+// `stream` around the wave kernel alone.
 template <typename Tsrc, typename T>
 cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t grid_rows,
-                       const int32_t* thick, const ApplyPass& pass, void* table,
+                       const int32_t* thick, const ApplyPass& pass, void* table, int* err,
                        cudaStream_t stream, cudaEvent_t ev_begin = nullptr,
                        cudaEvent_t ev_end = nullptr);
 
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
                          int32_t* place, cudaStream_t stream);
+
+// One matrix of a batch: size and offsets into the packed arrays (elements, not bytes).
+struct BatchMat {
+    int64_t n;
+    int64_t doff;    // diagonal (n), thick and place (n)
+    int64_t eoff;    // off-diagonal (n-1)
+    int64_t qoff;    // Q (n x n, leading dimension n)
+    int64_t goff;    // rotation grid ((n-1) x grid_layers (c,s) pairs)
+    int32_t cls;     // apply size class
+    int32_t pad;
+};
+
+// One flush of every unfinished matrix of a batch, one lane per matrix, lanes in `order`.
+cudaError_t launch_chase_batched(const BatchMat* mats, const int32_t* order, int32_t count,
+                                 ChaseState* states, double* d, double* e, double* grids,
+                                 int32_t* thick, int32_t* place, cudaStream_t stream);
+
+// Batched solve on device pointers (batched.cu); n, converged, iters are host arrays.
+int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t* n, double* d,
+                   double* e, double* Q, int32_t max_layers, double tol, int64_t maxiter_factor,
+                   int32_t exact_order, int32_t* converged, int64_t* iters, int64_t* rounds_out,
+                   double* ms_out);
+int batched_autotune(int device, cudaStream_t stream, double* ms);
+void batched_set_tuning(int64_t split, int32_t shape0, int32_t shape1);
+void batched_get_tuning(int64_t* split, int32_t* shape0, int32_t* shape1);
 
 }  // namespace symeig

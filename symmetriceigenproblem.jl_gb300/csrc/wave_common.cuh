@@ -1,0 +1,274 @@
+// wave_common.cuh -- the wave-window Givens tile shared by the single-matrix and the batched
+// apply kernels.
+//
+// A tile is the work of one CTA of 4 warps: 4 * (32/G) consecutive rows of Q, all columns of
+// the pass, all G*KB layers of the pass.
+//
+// Order of the rotations.  Rotation (i, L) acts on columns (i, i+1).  The reference's wave
+// order (src/wave.jl:62-162) applies (i, L) after (i-1, L) and after (i+1, L-1); per element
+// of Q that is the same sequence of rotations as the layer-major loop "for L, for i".  A
+// lane group walks waves t = 0, 1, 2, ... of its KB layers: wave t applies rotation
+// (t-1-l, l) for l = 0..KB-1, i.e. the column pairs (t-1-l, t-l) from right to left, which
+// respects both dependencies.  After wave t, column t-KB is final for the group.
+//
+// Layer groups.  The G groups of a row run in the G lane groups of one warp (32/G rows per
+// warp).  Group g lags group g-1 by KB+1 waves and receives its input columns from group g-1
+// through a warp shuffle, so a pass reads and writes each element of Q once.  All groups of a
+// warp hold the same rows, so the column read issued by every lane costs one sector per
+// warp; group 0 keeps it, group G-1 stores the finished column.
+//
+// (c,s) staging.  The table lays the rotations out per iteration: the G*KB pairs a warp needs
+// in iteration t are contiguous, each group's KB pairs padded by 16 bytes so that the
+// groups' pairs land in disjoint shared-memory banks.  Rotations outside the grid or above
+// a column's layer count are (1, 0), so the inner loop has no bounds logic.  The table is
+// cut into chunks of CH iterations that the CTA streams into a two-slot shared-memory ring
+// with cp.async.bulk (the TMA engine's bulk copy; no tensor map, no multicast), completion
+// tracked by one mbarrier per slot.  Every wait is bounded: after ~2 s of SM clock the tile
+// gives up and reports failure, and the kernel returns without touching Q again.
+//
+// Register window.  CH is a multiple of KB+1 and the chunk loop is fully unrolled, so column
+// t always lives in window slot t mod (KB+1), a compile-time constant: the window rotates
+// without register moves.  Group 0 keeps a second ring of KB+1 registers with the next
+// columns of Q, read KB+1 waves ahead.
+#pragma once
+
+#include "symeig_common.cuh"
+
+namespace symeig {
+namespace wave {
+
+constexpr int kThreads = 128;  // 4 warps per CTA
+
+template <typename T, int KB_, int G_>
+struct Shape {
+    using P2 = typename Pair<T>::type;
+    static constexpr int KB = KB_, G = G_, W = KB_ + 1;
+    static constexpr int RPW = 32 / G;                          // rows per warp
+    static constexpr int ROWS = RPW * (kThreads / 32);          // rows per tile
+    static constexpr int CH = (sizeof(T) == 8 ? 1 : 2) * W;     // iterations per chunk
+    static constexpr int GSTRIDE = KB * (int)sizeof(P2) + 16;   // bytes per group, padded
+    static constexpr int ITER = G * GSTRIDE;                    // bytes per iteration
+    static constexpr int CHUNK = CH * ITER;                     // bytes per chunk
+    static constexpr int LAYERS = KB * G;                       // layers per pass
+    static_assert(32 % G == 0, "groups must divide a warp");
+    static_assert(KB % 2 == 0, "pairs of slots are read together");
+    static_assert(CHUNK % 16 == 0 && GSTRIDE % 16 == 0, "bulk-copy alignment");
+    __host__ __device__ static int64_t iterations(int64_t n_loc) { return n_loc + KB + (int64_t)(G - 1) * W; }
+    __host__ __device__ static int64_t chunks(int64_t n_loc) { return (iterations(n_loc) + CH - 1) / CH; }
+    __host__ __device__ static int64_t table_bytes(int64_t n_loc) { return chunks(n_loc) * (int64_t)CHUNK; }
+};
+
+// ---- mbarrier / bulk-copy helpers (PTX) -----------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                 ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint64_t* bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(smem_u32(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+// Wait for phase `parity` of `bar`, giving up after ~2 s of SM clock.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity)
+{
+    if (mbar_test(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_test(bar, parity)) {
+        if (clock64() - t0 > 4000000000LL) return false;
+    }
+    return true;
+}
+
+// Store with a predicate, forced to a predicated instruction (no branch).
+__device__ __forceinline__ void st_pred(double* p, double v, bool pred)
+{
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.f64 [%0], %1;\n\t}"
+                 ::"l"(p), "d"(v), "r"((unsigned)pred));
+}
+__device__ __forceinline__ void st_pred(float* p, float v, bool pred)
+{
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.global.f32 [%0], %1;\n\t}"
+                 ::"l"(p), "f"(v), "r"((unsigned)pred));
+}
+
+// One table entry: iteration t, group g, slot l of a pass over columns [c0, c0+n_loc) and
+// layers [L0, L0+layers) of a Julia-layout grid with grid_rows rows.  place (may be null):
+// layer L of rotation i is (1,0) unless L < place[i].
+template <typename T, typename Sh, typename Tsrc>
+__device__ __forceinline__ void table_entry(unsigned char* table, int64_t t, int g, int l,
+                                            const Tsrc* grid, int64_t grid_rows,
+                                            const int32_t* place, int64_t c0, int64_t n_loc,
+                                            int64_t L0, int64_t layers)
+{
+    using P2 = typename Sh::P2;
+    const int64_t tg = t - (int64_t)g * Sh::W;
+    const int64_t i_loc = tg - 1 - l;
+    const int64_t lay = (int64_t)g * Sh::KB + l;
+    Tsrc c = Tsrc(1), s = Tsrc(0);
+    if (i_loc >= 0 && i_loc <= n_loc - 2 && lay < layers) {
+        const int64_t i = c0 + i_loc;
+        const int64_t L = L0 + lay;
+        if (place == nullptr || L < (int64_t)place[i]) {
+            const Tsrc* p = grid + 2 * (i + L * grid_rows);
+            c = p[0];
+            s = p[1];
+        }
+    }
+    P2 v;
+    v.x = (T)c;
+    v.y = (T)s;
+    *(P2*)(table + t * Sh::ITER + g * Sh::GSTRIDE + l * (int)sizeof(P2)) = v;
+}
+
+// The KB rotations of one wave on the window, (c,s) read from shared memory.  U is the wave's
+// slot (t mod (KB+1)); callers pass a constant of a fully unrolled loop, so every window
+// index folds to a constant and the window stays in registers.
+template <typename T, int KB>
+__device__ __forceinline__ void wave_rotations(T (&win)[KB + 1], const unsigned char* cs, const int U,
+                                               const T nz)
+{
+    constexpr int W = KB + 1;
+    if constexpr (sizeof(T) == 8) {
+#pragma unroll
+        for (int l = 0; l < KB; ++l) {
+            const double2 p = *reinterpret_cast<const double2*>(cs + l * 16);
+            rot_fma(win[(U - 1 - l + 2 * W) % W], win[(U - l + 2 * W) % W], p.x, p.y, nz);
+        }
+    } else {
+#pragma unroll
+        for (int l = 0; l < KB; l += 2) {
+            const float4 p = *reinterpret_cast<const float4*>(cs + l * 8);
+            rot(win[(U - 1 - l + 2 * W) % W], win[(U - l + 2 * W) % W], p.x, p.y);
+            rot(win[(U - 2 - l + 2 * W) % W], win[(U - 1 - l + 2 * W) % W], p.z, p.w);
+        }
+    }
+}
+
+// CTA-shared staging state of the tile loop: the two-slot ring and one mbarrier per slot,
+// with the number of completed waits per slot (their parity is the phase to wait for next).
+template <typename Sh>
+struct Staging {
+    unsigned char (*ring)[Sh::CHUNK];
+    uint64_t* bar;
+    uint32_t uses0, uses1;
+};
+
+template <typename Sh>
+__device__ __forceinline__ void staging_init(Staging<Sh>& st)
+{
+    if (threadIdx.x == 0) {
+        mbar_init(&st.bar[0], 1);
+        mbar_init(&st.bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    st.uses0 = st.uses1 = 0;
+    __syncthreads();
+}
+
+// One tile: rows [row0, row0 + ROWS) of Q (m rows, leading dimension ldq, columns
+// [0, n_loc) of the pass) through the n_chunks chunks of `table`.  Every thread of the CTA
+// calls it.  Returns false (all threads) when a bounded wait gave up.
+template <typename T, typename Sh>
+__device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_t m, int64_t row0,
+                                          int32_t n_loc, const unsigned char* __restrict__ table,
+                                          int32_t n_chunks, const T nz, Staging<Sh>& st)
+{
+    constexpr int KB = Sh::KB, G = Sh::G, CH = Sh::CH, W = Sh::W, RPW = Sh::RPW;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        bulk_load(st.ring[0], table, Sh::CHUNK, &st.bar[0]);
+        if (n_chunks > 1) bulk_load(st.ring[1], table + Sh::CHUNK, Sh::CHUNK, &st.bar[1]);
+    }
+
+    const int lane = tid & 31;
+    const int g = lane / RPW;
+    const int rl = lane - g * RPW;
+    const int64_t row = row0 + (tid >> 5) * RPW + rl;
+    const bool row_ok = row < m;
+    T* __restrict__ qrow = Q + (row_ok ? row : 0);
+    const bool storer = (g == G - 1) && row_ok;  // group G-1 writes Q
+    const int lag = g * W;                       // waves this group trails group 0
+
+    T win[W], ahead[W];
+#pragma unroll
+    for (int q = 0; q < W; ++q) {
+        win[q] = T(0);
+        ahead[q] = (q < n_loc) ? qrow[(int64_t)q * ldq] : T(0);
+    }
+    T xout = T(0);
+
+    for (int32_t c = 0; c < n_chunks; ++c) {
+        const int b = c & 1;
+        const uint32_t parity = ((b ? st.uses1 : st.uses0) + (uint32_t)(c >> 1)) & 1u;
+        const bool ok = mbar_wait_bounded(&st.bar[b], parity);
+        if (__syncthreads_or(!ok)) return false;
+        const unsigned char* sb = st.ring[b] + g * Sh::GSTRIDE;
+        const int32_t t0 = c * CH;
+        // column t0 + u + W is read in iteration u; group G-1 writes column t0 + u - lag - KB
+        const int32_t st0 = t0 - lag - KB;
+        const T* ld_base = qrow + (int64_t)(t0 + W) * ldq;
+        T* st_base = qrow + (int64_t)st0 * ldq;
+        const bool interior = (t0 + W + CH <= n_loc) && (t0 - (G - 1) * W - KB >= 0) &&
+                              (t0 - KB + CH <= n_loc);
+        if (interior) {
+#pragma unroll
+            for (int u = 0; u < CH; ++u) {
+                const T up = __shfl_up_sync(0xffffffffu, xout, RPW);
+                const T xin = (g == 0) ? ahead[u % W] : up;
+                ahead[u % W] = ld_base[(int64_t)u * ldq];
+                win[u % W] = xin;
+                wave_rotations<T, KB>(win, sb + u * Sh::ITER, u % W, nz);
+                xout = win[(u + 1) % W];
+                st_pred(st_base + (int64_t)u * ldq, xout, storer);
+            }
+        } else {
+            const int32_t ld_cnt = min(max(n_loc - t0 - W, 0), CH);
+            const int32_t st_lo = max(-st0, 0);
+            const int32_t st_hi = min(n_loc - st0, CH);
+#pragma unroll
+            for (int u = 0; u < CH; ++u) {
+                const T up = __shfl_up_sync(0xffffffffu, xout, RPW);
+                const T xin = (g == 0) ? ahead[u % W] : up;
+                T nxt = T(0);
+                if (u < ld_cnt) nxt = ld_base[(int64_t)u * ldq];
+                ahead[u % W] = nxt;
+                win[u % W] = xin;
+                wave_rotations<T, KB>(win, sb + u * Sh::ITER, u % W, nz);
+                xout = win[(u + 1) % W];
+                st_pred(st_base + (int64_t)u * ldq, xout, storer && u >= st_lo && u < st_hi);
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && c + 2 < n_chunks) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            bulk_load(st.ring[b], table + (int64_t)(c + 2) * Sh::CHUNK, Sh::CHUNK, &st.bar[b]);
+        }
+    }
+    st.uses0 += (uint32_t)((n_chunks + 1) >> 1);
+    st.uses1 += (uint32_t)(n_chunks >> 1);
+    return true;
+}
+
+}  // namespace wave
+}  // namespace symeig

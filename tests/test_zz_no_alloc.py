@@ -52,7 +52,7 @@ def test_noalloc_matches_handle_entry_two_calls(cuda, pkg, m, n, k):
 def test_noalloc_rejects_sizes_beyond_its_array(cuda, pkg):
     torch = cuda
     lib = pkg.load_library()
-    n, m, k = 40000, 1, 1       # (n + 71) * 1024 bytes > 32 MiB
+    n, m, k = 40000, 1, 1       # ceil((n + 71) / 9) * 10368 bytes > 32 MiB
     A = torch.zeros(n, dtype=torch.float64, device="cuda")
     cs = torch.zeros(2 * (n - 1), dtype=torch.float64, device="cuda")
     rc = lib.symeig_apply_givens_f64_noalloc(ctypes.c_void_p(A.data_ptr()), 1, m, n,
