@@ -153,6 +153,24 @@ int symeig_batched_autotune(symeig_handle h, double* ms);
 /* Read (set = 0) or write (set != 0) the batched tuning: class split and shape per class. */
 int symeig_batched_tuning(int64_t* split, int32_t* shape_small, int32_t* shape_large, int32_t set);
 
+/* ---- adjoint (reverse-mode derivative) of the eigensolve ------------------------------------ *
+ * No reference counterpart (the reference has no derivatives); this is the pullback behind
+ * the Julia ChainRulesCore rrule and the torch autograd Function of the host bindings.
+ * For count matrices of order n (back to back): eigenvalues lam (n each, in the order the
+ * solver returns them, i.e. unsorted like H.dv), eigenvectors Q (n x n column-major,
+ * leading dimension n, the solver's output), loss gradients glam (n) and gQ (n x n, or NULL
+ * for a loss of the eigenvalues only).  Writes dL/dd (gd, n each) and dL/de (ge, n-1 each):
+ *   M = diag(glam) + F o (Q^T gQ), F_ij = 1/(lam_j - lam_i) (0 on the diagonal and where
+ *   lam_i == lam_j), Abar = Q M Q^T, dL/dd_i = Abar_ii, dL/de_i = Abar_{i,i+1} + Abar_{i+1,i}.
+ * Q^T gQ and Q M run on the FP64 tensor cores (mma.sync .f64) with the F-masking and the
+ * (off-)diagonal extraction fused into their epilogues; Abar is never formed. */
+int symeig_eig_adjoint_f64(symeig_handle h, int64_t count, int64_t n, const double* lam,
+                           const double* Q, const double* glam, const double* gQ, double* gd,
+                           double* ge);
+int symeig_eig_adjoint_f64_dev(symeig_handle h, int64_t count, int64_t n, const double* lam,
+                               const double* Q, const double* glam, const double* gQ, double* gd,
+                               double* ge);
+
 /* ---- bulk apply without any allocation -------------------------------------------------- *
  * No counterpart in the reference.  For callers that cannot allocate device memory at call
  * time (their device memory belongs to another allocator that reserved it up front, or

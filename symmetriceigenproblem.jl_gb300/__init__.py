@@ -9,6 +9,7 @@ from .api import (  # noqa: F401
     SymTridiagonal,
     bulk_wave_order_2x2_rmul_,
     bulk_wave_order_2x2_rmul_parallel_,
+    eig_adjoint,
     batched_autotune,
     qr_algorithm_batched_,
     eigen_decomp_,
@@ -17,3 +18,8 @@ from .api import (  # noqa: F401
 )
 from ._lib import Handle, SymeigError, default_handle, load as load_library  # noqa: F401
 from .build import build, LIB as LIBRARY_PATH  # noqa: F401
+
+try:  # the autograd Functions need torch
+    from .api import TridiagEigh, TridiagEighBatched  # noqa: F401
+except ImportError:  # pragma: no cover
+    pass

@@ -261,3 +261,95 @@ def batched_autotune(handle: Handle | None = None):
     split, s0, s1 = c_i64(), c_i32(), c_i32()
     h._lib.symeig_batched_tuning(ctypes.byref(split), ctypes.byref(s0), ctypes.byref(s1), 0)
     return {"split": split.value, "shape_small": s0.value, "shape_large": s1.value}, [list(ms[0:2]), list(ms[2:4])]
+
+
+def eig_adjoint(lam, Q, glam, gQ=None, handle: Handle | None = None):
+    """dL/d(d, e) of the tridiagonal eigensolve from dL/dlam and dL/dQ (symeig_eig_adjoint_f64*).
+
+    Single matrix: lam (n,), Q (n, n) column-major, glam (n,), gQ (n, n) or None.  Batch of B
+    matrices of one order: lam (B, n), Q (B, n, n) with each Q[b] column-major (i.e.
+    Q[b].stride(0) == 1), glam (B, n), gQ like Q or None.  numpy (host) or CUDA torch (device).
+    Returns (gd, ge) with shapes (n,), (n-1,) or (B, n), (B, n-1)."""
+    dev = _is_torch(lam)
+    batched = lam.ndim == 2
+    B = int(lam.shape[0]) if batched else 1
+    n = int(lam.shape[-1])
+    h = handle or default_handle(lam.device.index if dev else 0)
+
+    def colmajor_flat(M):
+        # the column-major memory of each n x n matrix, back to back
+        if dev:
+            return (M.transpose(-1, -2).contiguous() if M.ndim == 2 else M.transpose(-1, -2).contiguous()).reshape(-1)
+        return np.ascontiguousarray(np.swapaxes(M, -1, -2)).reshape(-1)
+
+    if dev:
+        zl = lambda *s: torch.empty(*s, dtype=torch.float64, device=lam.device)
+        lam_c, glam_c = lam.contiguous().reshape(-1), glam.contiguous().reshape(-1)
+        Qf = colmajor_flat(Q)
+        gQf = colmajor_flat(gQ) if gQ is not None else None
+        gd, ge = zl(B * n), zl(max(B * (n - 1), 1))
+        ptr = lambda a: ctypes.c_void_p(a.data_ptr() if a is not None else None)
+        with h.on_stream(torch.cuda.current_stream(lam.device).cuda_stream):
+            h.call("symeig_eig_adjoint_f64_dev", B, n, ptr(lam_c), ptr(Qf), ptr(glam_c), ptr(gQf), ptr(gd), ptr(ge))
+    else:
+        lam_c = np.ascontiguousarray(lam, dtype=np.float64).reshape(-1)
+        glam_c = np.ascontiguousarray(glam, dtype=np.float64).reshape(-1)
+        Qf = colmajor_flat(np.asarray(Q, dtype=np.float64))
+        gQf = colmajor_flat(np.asarray(gQ, dtype=np.float64)) if gQ is not None else None
+        gd, ge = np.empty(B * n), np.empty(max(B * (n - 1), 1))
+        ptr = lambda a: ctypes.c_void_p(a.ctypes.data if a is not None else None)
+        h.call("symeig_eig_adjoint_f64", B, n, ptr(lam_c), ptr(Qf), ptr(glam_c), ptr(gQf), ptr(gd), ptr(ge))
+    ge = ge[: B * (n - 1)]
+    if batched:
+        return gd.reshape(B, n), ge.reshape(B, n - 1)
+    return gd, ge
+
+
+if torch is not None:
+    class TridiagEigh(torch.autograd.Function):
+        """(lam, Q) = eigen-decomposition of SymTridiagonal(d, e) by the GB300 qr_algorithm!,
+        differentiable: the backward is symeig_eig_adjoint_f64_dev.  lam is unsorted (as
+        H.dv of the reference); Q is returned as a column-major view.  The counterpart of the
+        Julia ChainRulesCore rrule of the Julia binding."""
+
+        @staticmethod
+        def forward(ctx, d, e):
+            n = d.shape[0]
+            dd, ee = d.detach().clone().contiguous(), e.detach().clone().contiguous()
+            Q = torch.eye(n, dtype=torch.float64, device=d.device).T.contiguous().T
+            _, conv, _ = qr_algorithm_(SymTridiagonal(dd, ee), Q)
+            if not conv:
+                raise RuntimeError("qr_algorithm! did not converge")
+            ctx.save_for_backward(dd, Q)
+            return dd, Q
+
+        @staticmethod
+        def backward(ctx, glam, gQ):
+            lam, Q = ctx.saved_tensors
+            if glam is None:
+                glam = torch.zeros_like(lam)
+            gd, ge = eig_adjoint(lam, Q, glam.contiguous(), gQ)
+            return gd, ge
+
+    class TridiagEighBatched(torch.autograd.Function):
+        """Batched TridiagEigh: d (B, n), e (B, n-1) -> lam (B, n), Q (B, n, n) (each Q[b]
+        column-major), via symeig_qr_batched_f64_dev and the batched adjoint."""
+
+        @staticmethod
+        def forward(ctx, d, e):
+            B, n = d.shape
+            dd, ee = d.detach().clone().contiguous(), e.detach().clone().contiguous()
+            Qf = torch.eye(n, dtype=torch.float64, device=d.device).reshape(1, n, n).repeat(B, 1, 1).reshape(-1)
+            conv, _ = qr_algorithm_batched_(dd.reshape(-1), ee.reshape(-1), [n] * B, Qf)
+            if not conv.all():
+                raise RuntimeError("qr_algorithm! did not converge")
+            Q = Qf.reshape(B, n, n).transpose(1, 2)   # column-major per matrix
+            ctx.save_for_backward(dd, Q)
+            return dd, Q
+
+        @staticmethod
+        def backward(ctx, glam, gQ):
+            lam, Q = ctx.saved_tensors
+            if glam is None:
+                glam = torch.zeros_like(lam)
+            return eig_adjoint(lam, Q, glam.contiguous(), gQ)

@@ -630,6 +630,57 @@ int symeig_batched_tuning(int64_t* split, int32_t* shape_small, int32_t* shape_l
     return SYMEIG_OK;
 }
 
+int symeig_eig_adjoint_f64_dev(symeig_handle h, int64_t count, int64_t n, const double* lam,
+                               const double* Q, const double* glam, const double* gQ, double* gd,
+                               double* ge)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (count < 0 || n < 0 || (count > 0 && n > (1 << 20))) return SYMEIG_ERR_SIZE;
+    if (count == 0 || n == 0) return SYMEIG_OK;
+    if (!lam || !Q || !glam || !gd || (n > 1 && !ge)) return SYMEIG_ERR_NULL;
+    begin_call(h);
+    if (gQ) CK(h->cs.ensure((size_t)adjoint_scratch_doubles(count, n) * sizeof(double)));
+    auto t0 = std::chrono::steady_clock::now();
+    rc = adjoint_dev(h->stream, count, n, lam, Q, glam, gQ, gd, ge, (double*)h->cs.ptr);
+    h->stats.total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+int symeig_eig_adjoint_f64(symeig_handle h, int64_t count, int64_t n, const double* lam,
+                           const double* Q, const double* glam, const double* gQ, double* gd,
+                           double* ge)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (count < 0 || n < 0 || (count > 0 && n > (1 << 20))) return SYMEIG_ERR_SIZE;
+    if (count == 0 || n == 0) return SYMEIG_OK;
+    if (!lam || !Q || !glam || !gd || (n > 1 && !ge)) return SYMEIG_ERR_NULL;
+    cudaStream_t s = h->stream;
+    const size_t nn = (size_t)count * n * n, nv = (size_t)count * n, ne = (size_t)count * (n - 1);
+    // device staging: Q and gQ in q (2 nn), lam/glam/gd in d (3 nv), ge in e
+    CK(h->q.ensure((gQ ? 2 : 1) * nn * sizeof(double)));
+    CK(h->d.ensure(3 * nv * sizeof(double)));
+    CK(h->e.ensure(std::max<size_t>(ne, 1) * sizeof(double)));
+    double* dq = (double*)h->q.ptr;
+    double* dgq = gQ ? dq + nn : nullptr;
+    double* dl = (double*)h->d.ptr;
+    double* dgl = dl + nv;
+    double* dgd = dl + 2 * nv;
+    double* dge = (double*)h->e.ptr;
+    CK(cudaMemcpyAsync(dq, Q, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (gQ) CK(cudaMemcpyAsync(dgq, gQ, nn * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dl, lam, nv * sizeof(double), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(dgl, glam, nv * sizeof(double), cudaMemcpyHostToDevice, s));
+    rc = symeig_eig_adjoint_f64_dev(h, count, n, dl, dq, dgl, dgq, dgd, dge);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(gd, dgd, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (ne) CK(cudaMemcpyAsync(ge, dge, ne * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return SYMEIG_OK;
+}
+
 int symeig_eigen_decomp_f64(symeig_handle h, double* d, double* e, int64_t n, double* Q,
                             int64_t ldq, int32_t* converged, int64_t* iter)
 {

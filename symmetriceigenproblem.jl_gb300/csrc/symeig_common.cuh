@@ -126,6 +126,10 @@ int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t
                    int32_t exact_order, int32_t* converged, int64_t* iters, int64_t* rounds_out,
                    double* ms_out);
 int batched_autotune(int device, cudaStream_t stream, double* ms);
+// Adjoint of the eigensolve for count matrices of order n (adjoint.cu).
+int adjoint_dev(cudaStream_t s, int64_t count, int64_t n, const double* lam, const double* Q,
+                const double* glam, const double* gQ, double* gd, double* ge, double* scratch);
+int64_t adjoint_scratch_doubles(int64_t count, int64_t n);
 void batched_set_tuning(int64_t split, int32_t shape0, int32_t shape1);
 void batched_get_tuning(int64_t* split, int32_t* shape0, int32_t* shape1);
 
