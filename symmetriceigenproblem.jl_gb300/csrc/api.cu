@@ -195,6 +195,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     init.grid_layers = grid_layers;
     init.exact_order = h->exact_order;
     init.status = CHASE_RUNNING;
+    init.neg_zero = -0.0;
     ChaseState* dstate = (ChaseState*)h->state.ptr;
 
     cudaStream_t ms = h->stream, cs = h->chase_stream;

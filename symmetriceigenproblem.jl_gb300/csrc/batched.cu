@@ -295,6 +295,7 @@ int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t
         s.grid_layers = grid_layers;
         s.exact_order = exact_order;
         s.status = CHASE_RUNNING;
+        s.neg_zero = -0.0;
         states[i] = s;
     }
     // lanes in order of decreasing n (stable), so that a warp's chases have similar lengths

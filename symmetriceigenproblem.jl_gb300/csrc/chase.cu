@@ -26,6 +26,49 @@ namespace {
 
 __device__ __forceinline__ double jl_max(double a, double b) { return (a > b || a != a) ? a : b; }
 
+// ---- bit-pattern tests on the integer pipe ----------------------------------------------
+// On GB300 every FP64 instruction, compares included, occupies the FP64 unit for ~64 cycles;
+// these give the same answers as the IEEE comparisons they replace.
+__device__ __forceinline__ uint64_t abs_bits(double x)
+{
+    return (uint64_t)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ bool nan_bits(uint64_t a) { return a > 0x7FF0000000000000ull; }
+__device__ __forceinline__ double neg(double x)
+{
+    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+// x < 0.0
+__device__ __forceinline__ bool is_negative(double x)
+{
+    const uint64_t b = (uint64_t)__double_as_longlong(x), a = b & 0x7FFFFFFFFFFFFFFFull;
+    return (b >> 63) != 0 && a != 0 && !nan_bits(a);
+}
+// a*b as an FMA with a -0.0 addend supplied at run time: bit-identical to the product, and an
+// FP64 FMA issues faster than an FP64 multiply on GB300.
+__device__ __forceinline__ double mulz(double a, double b, double nz) { return __fma_rn(a, b, nz); }
+
+// Which branch of givensAlgorithm (f, g) takes: 0 g == 0, 1 f == 0, 2 scaled down,
+// 3 scaled up, 4 plain (also when f or g is NaN: the NaN scale fails both range tests).
+__device__ __forceinline__ int givens_case(double f, double g)
+{
+    const uint64_t af = abs_bits(f), ag = abs_bits(g);
+    if (ag == 0) return 0;
+    if (af == 0) return 1;
+    if (nan_bits(af) || nan_bits(ag)) return 4;
+    const uint64_t m = af > ag ? af : ag;
+    if (m >= 0x5E40000000000000ull) return 2;  // max(|f|,|g|) >= 2^485
+    if (m <= 0x21A0000000000000ull) return 3;  // max(|f|,|g|) <= 2^-485
+    return 4;
+}
+
+// The sign convention of givensAlgorithm: flip (c, s, r) when |f| > |g| and c < 0.
+__device__ __forceinline__ bool givens_flip(double f, double g, double c)
+{
+    const uint64_t af = abs_bits(f), ag = abs_bits(g);
+    return af > ag && !nan_bits(af) && !nan_bits(ag) && is_negative(c);
+}
+
 // LinearAlgebra.givensAlgorithm (LAPACK 3.2 DLARTG port), as called by get_rotation.
 __device__ __forceinline__ void givens(double f, double g, double& cs, double& sn, double& r)
 {
@@ -173,6 +216,153 @@ __device__ void single_shift(double* __restrict__ dv, double* __restrict__ ev, i
     }
 }
 
+// ---- the sweep on two warps ------------------------------------------------------------------
+//
+// single_shift! is one dependency chain per step: (f, g) -> r = sqrt(f^2 + g^2) -> c = f/r,
+// s = g/r -> the 2x2 update -> next (f, g).  On GB300 each FP64 instruction holds its SM
+// sub-partition's FP64 unit ~64 cycles, so the step time is the number of FP64 instructions
+// the chain's warp issues.  Two warps on two sub-partitions split a step:
+//   warp 0 (the chain): f*f, sqrt, c = f/r, s*B21, s*B22, B11', B12', B11'*s, B12'' -> next f;
+//   warp 1: s = g/r, next bulge (= next g) and its square, next B21, the B21'/B22'/B22''
+//           updates (-> next B11), B11'', every store and the rotation record.
+// They trade values through a two-slot shared mailbox (slot = step parity) and five named
+// barriers, each used producer -> consumer (bar.arrive / bar.sync) except the (c, s)
+// exchange.  Every value and every rounding is the one the one-thread sweep computes.
+enum : int { kBarR = 1, kBarCS = 2, kBarG = 3, kBarB = 4, kBarP = 5 };
+
+struct Mail {
+    double r, f;            // warp 0 -> 1 (kBarR)
+    double c, s;            // exchanged (kBarCS)
+    double bulge, e_next, gg;  // warp 1 -> 0 (kBarG): next g, next B21, next g*g
+    double b22pp;           // warp 1 -> 0 (kBarB): next B11
+    double b11p, b12p, b12pp;  // warp 0 -> 1 (kBarP)
+    int mode;               // 0: warp 1 divides; 1: warp 0 ran the full givensAlgorithm
+};
+
+__device__ __forceinline__ void nb_sync(int id)
+{
+    asm volatile("bar.sync %0, 64;" ::"r"(id) : "memory");
+}
+__device__ __forceinline__ void nb_arrive(int id)
+{
+    asm volatile("bar.arrive %0, 64;" ::"r"(id) : "memory");
+}
+
+// single_shift!(H, from, to, mu, givens, layer_thickness) (src/bulge_chasing.jl:11-144) by
+// both warps of the CTA.  Step i (1-based, from .. to-1) is the reference's first rotation
+// for i = from and its loop body otherwise; both have the same 2x2 update.
+__device__ void single_shift_2w(double* __restrict__ dv, double* __restrict__ ev, int64_t from,
+                                int64_t to, double mu, double* __restrict__ grid,
+                                int32_t* __restrict__ thick, int32_t* __restrict__ place,
+                                int64_t rows, int32_t layer, double nz, Mail* mail)
+{
+    const int warp = threadIdx.x >> 5;
+    const bool lead = (threadIdx.x & 31) == 0;
+    const double H11 = dv[from - 1], H21 = ev[from - 1];
+    double B11 = H11, B21 = H21;
+    double B22n = dv[from];                                  // dv[i+1] (1-based) for step i
+    double B23n = (from + 2 <= to) ? ev[from] : 0.0;         // ev[i+1] (1-based) for step i
+    if (warp == 0) {
+        double f = __dsub_rn(H11, mu), g = H21, gg = mulz(H21, H21, nz);
+        for (int64_t i = from; i <= to - 1; ++i) {
+            Mail& mb = mail[i & 1];
+            const double B22 = B22n;
+            if (i + 1 <= to - 1) B22n = dv[i + 1];
+            if (i > from) {
+                nb_sync(kBarG);
+                const Mail& pv = mail[(i - 1) & 1];
+                g = pv.bulge;
+                B21 = pv.e_next;
+                gg = pv.gg;
+            }
+            double c, s, r;
+            const int mode = givens_case(f, g) == 4 ? 0 : 1;
+            if (mode == 0) {
+                r = __dsqrt_rn(__dadd_rn(mulz(f, f, nz), gg));
+                mb.r = r; mb.f = f; mb.mode = 0;
+                nb_arrive(kBarR);
+                c = __ddiv_rn(f, r);
+                mb.c = c;
+            } else {
+                givens(f, g, c, s, r);
+                mb.r = r; mb.f = f; mb.mode = 1; mb.c = c; mb.s = s;
+                nb_arrive(kBarR);
+            }
+            nb_sync(kBarCS);
+            if (mode == 0) {
+                s = mb.s;
+                if (givens_flip(f, g, c)) { c = neg(c); s = neg(s); }
+            }
+            if (i > from) {
+                nb_sync(kBarB);
+                B11 = mail[(i - 1) & 1].b22pp;
+            }
+            const double sB21 = mulz(s, B21, nz), sB22 = mulz(s, B22, nz);
+            const double B11p = __fma_rn(c, B11, sB21);
+            const double B12p = __fma_rn(c, B21, sB22);
+            const double B12pp = __fma_rn(B12p, c, neg(mulz(B11p, s, nz)));
+            mb.b11p = B11p; mb.b12p = B12p; mb.b12pp = B12pp;
+            nb_arrive(kBarP);
+            f = B12pp;
+        }
+    } else {
+        double g = H21;
+        for (int64_t i = from; i <= to - 1; ++i) {
+            Mail& mb = mail[i & 1];
+            const double B22 = B22n, B23 = B23n;
+            if (i + 1 <= to - 1) B22n = dv[i + 1];
+            if (i + 3 <= to) B23n = ev[i + 1];
+            nb_sync(kBarR);
+            double r = mb.r;
+            const double f = mb.f;
+            const int mode = mb.mode;
+            double s = 0.0;
+            if (mode == 0) {
+                s = __ddiv_rn(g, r);
+                mb.s = s;
+            }
+            nb_sync(kBarCS);
+            double c = mb.c;
+            if (mode == 0) {
+                if (givens_flip(f, g, c)) { c = neg(c); s = neg(s); r = neg(r); }
+            } else {
+                s = mb.s;
+            }
+            double bulge = 0.0, e_next = 0.0;
+            if (i + 2 <= to) {
+                bulge = mulz(s, B23, nz);
+                e_next = mulz(c, B23, nz);
+            }
+            if (i < to - 1) {
+                mb.bulge = bulge; mb.e_next = e_next; mb.gg = mulz(bulge, bulge, nz);
+                nb_arrive(kBarG);
+            }
+            const double sB11 = mulz(s, B11, nz), sB21 = mulz(s, B21, nz);
+            const double B21p = __fma_rn(c, B21, neg(sB11));
+            const double B22p = __fma_rn(c, B22, neg(sB21));
+            const double B22pp = __fma_rn(B22p, c, neg(mulz(B21p, s, nz)));
+            if (i < to - 1) {
+                mb.b22pp = B22pp;
+                nb_arrive(kBarB);
+            }
+            nb_sync(kBarP);
+            const double B11p = mb.b11p, B12p = mb.b12p, B12pp = mb.b12pp;
+            const double B11pp = __fma_rn(B11p, c, mulz(B12p, s, nz));
+            if (lead) {
+                if (i > from) ev[i - 2] = r;
+                dv[i - 1] = B11pp;
+                dv[i] = B22pp;
+                ev[i - 1] = B12pp;
+                if (i + 2 <= to) ev[i] = e_next;
+                record(grid, thick, place, rows, i, layer, c, s);
+            }
+            g = bulge;
+            B11 = B22pp;
+            B21 = e_next;
+        }
+    }
+}
+
 __device__ __forceinline__ int32_t warp_max(int32_t v)
 {
 #pragma unroll
@@ -182,6 +372,8 @@ __device__ __forceinline__ int32_t warp_max(int32_t v)
 
 // One flush: the reference's inner loop from `to = last_block_ends_at` until the matrix is
 // split into converged parts, every block has reached max_layers, or iter > maxiter.
+// Warp 0 runs the control flow and the O(n) scans with ballots; each sweep runs on both
+// warps (single_shift_2w).
 //
 // Exact-order placement (st->exact_order != 0).  The reference applies a flush's grid in
 // layer-major order, which equals the order the chase made the rotations only while every
@@ -192,14 +384,25 @@ __device__ __forceinline__ int32_t warp_max(int32_t v)
 // and skipped slots are set to (1,0), so the layer-major order of the grid is the chase's
 // order.  The chase itself (and so every eigenvalue) is the reference's.  A sweep whose layer
 // would exceed the grid's capacity ends the flush early (st->early_flushes counts these).
-__global__ void __launch_bounds__(32, 1)
+struct Decision {
+    int64_t from, to;
+    double mu;
+    int32_t layer;
+    int32_t action;  // 0 stop, 1 sweep, 2 no sweep this iteration
+};
+
+__global__ void __launch_bounds__(64, 1)
 chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __restrict__ ev,
              double* __restrict__ grid, int32_t* __restrict__ thick, int32_t* __restrict__ place)
 {
-    const int lane = threadIdx.x;
+    __shared__ Mail mail[2];
+    __shared__ Decision dec;
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
     const int64_t n = st->n;
     const int64_t start = st->start;
     const double tol = st->tol;
+    const double nz = st->neg_zero;
     const int32_t max_layers = st->max_layers;
     const int32_t grid_layers = st->grid_layers;
     const bool exact = st->exact_order != 0;
@@ -208,11 +411,11 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
     int64_t lbe = st->last_block_ends_at;
     const int64_t rows = n > 1 ? n - 1 : 1;
 
-    for (int64_t q = lane; q < n; q += 32) {
+    for (int64_t q = threadIdx.x; q < n; q += 64) {
         thick[q] = 0;
         place[q] = 0;
     }
-    __syncwarp();
+    __syncthreads();
 
     bool did = false;
     int64_t rotations = 0, min_from = n + 1, max_to = 0, early = 0;
@@ -220,79 +423,100 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
     int64_t to = lbe;
 
     for (;;) {
-        if (iter > maxiter) { status = CHASE_MAXITER; break; }
-        if (to <= start) break;
-        // from = largest j+1 with is_small(j), j in [start, to-1]; start if none
-        int64_t from = start;
-        for (int64_t base = to - 1; base >= start; base -= 32) {
-            const int64_t j = base - lane;
-            const bool sm = (j >= start) && is_small(dv, ev, j, tol);
-            const unsigned mask = __ballot_sync(0xffffffffu, sm);
-            if (mask) { from = base - (__ffs(mask) - 1) + 1; break; }
-        }
-        if (from == to) {
-            if (lane == 0) ev[from - 2] = 0.0;
-            if (to == lbe) lbe -= 1;
-            to -= 1;
-        } else {
-            int32_t mx = 0;
-            for (int64_t q = from - 1 + lane; q <= to - 1; q += 32) mx = max(mx, thick[q]);
-            mx = warp_max(mx);
-            if (mx == max_layers) {
-                to = from - 1;
+        if (warp == 0) {
+            Decision d{0, 0, 0.0, 0, 2};
+            if (iter > maxiter) {
+                status = CHASE_MAXITER;
+                d.action = 0;
+            } else if (to <= start) {
+                d.action = 0;
             } else {
-                int32_t layer = 0;
-                if (exact) {
-                    int32_t L = 0;
-                    for (int64_t q = from - 1 + lane; q <= to - 2; q += 32) L = max(L, place[q]);
-                    L = warp_max(L);
-                    if (to <= n - 1) L = max(L, place[to - 1]);
-                    if (from >= 2) L = max(L, place[from - 2] - 1);
-                    layer = L + 1;
-                    if (layer > grid_layers) { early = 1; break; }
-                    // slots skipped by the jump to `layer` hold the identity
-                    for (int64_t q = from - 1 + lane; q <= to - 2; q += 32)
-                        for (int32_t g = place[q] + 1; g < layer; ++g) {
-                            double* p = grid + 2 * (q + (int64_t)(g - 1) * rows);
-                            p[0] = 1.0;
-                            p[1] = 0.0;
+                // from = largest j+1 with is_small(j), j in [start, to-1]; start if none
+                int64_t from = start;
+                for (int64_t base = to - 1; base >= start; base -= 32) {
+                    const int64_t j = base - lane;
+                    const bool sm = (j >= start) && is_small(dv, ev, j, tol);
+                    const unsigned mask = __ballot_sync(0xffffffffu, sm);
+                    if (mask) { from = base - (__ffs(mask) - 1) + 1; break; }
+                }
+                if (from == to) {
+                    if (lane == 0) ev[from - 2] = 0.0;
+                    if (to == lbe) lbe -= 1;
+                    to -= 1;
+                } else {
+                    int32_t mx = 0;
+                    for (int64_t q = from - 1 + lane; q <= to - 1; q += 32) mx = max(mx, thick[q]);
+                    mx = warp_max(mx);
+                    if (mx == max_layers) {
+                        to = from - 1;
+                    } else {
+                        int32_t layer = 0;
+                        bool go = true;
+                        if (exact) {
+                            int32_t L = 0;
+                            for (int64_t q = from - 1 + lane; q <= to - 2; q += 32) L = max(L, place[q]);
+                            L = warp_max(L);
+                            if (to <= n - 1) L = max(L, place[to - 1]);
+                            if (from >= 2) L = max(L, place[from - 2] - 1);
+                            layer = L + 1;
+                            if (layer > grid_layers) {
+                                early = 1;
+                                go = false;
+                                d.action = 0;
+                            } else {
+                                // slots skipped by the jump to `layer` hold the identity
+                                for (int64_t q = from - 1 + lane; q <= to - 2; q += 32)
+                                    for (int32_t g = place[q] + 1; g < layer; ++g) {
+                                        double* p = grid + 2 * (q + (int64_t)(g - 1) * rows);
+                                        p[0] = 1.0;
+                                        p[1] = 0.0;
+                                    }
+                            }
                         }
-                    __syncwarp();
+                        if (go) {
+                            d.mu = wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
+                            d.from = from;
+                            d.to = to;
+                            d.layer = layer;
+                            d.action = 1;
+                            did = true;
+                            iter += 1;
+                            rotations += to - from;
+                            min_from = min(min_from, from);
+                            max_to = max(max_to, to);
+                        }
+                    }
                 }
-                if (lane == 0) {
-                    const double mu = wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
-                    single_shift(dv, ev, from, to, mu, grid, thick, place, rows, layer);
-                }
-                did = true;
-                iter += 1;
-                rotations += to - from;
-                min_from = min(min_from, from);
-                max_to = max(max_to, to);
+                if (d.action == 2 && to <= start) d.action = 0;
             }
+            if (lane == 0) dec = d;
         }
-        __syncwarp();
-        if (to <= start) break;
+        __syncthreads();
+        const Decision d = dec;
+        if (d.action == 1)
+            single_shift_2w(dv, ev, d.from, d.to, d.mu, grid, thick, place, rows, d.layer, nz, mail);
+        __syncthreads();
+        if (d.action == 0) break;  // both warps leave on the same decision
     }
-    __syncwarp();
 
-    int32_t kmax = 0;
-    for (int64_t q = lane; q < n; q += 32) kmax = max(kmax, place[q]);
-    kmax = warp_max(kmax);
-
-    if (lane == 0) {
-        if (status == CHASE_RUNNING) status = did ? CHASE_FLUSH : CHASE_CONVERGED;
-        st->status = status;
-        st->iter = iter;
-        st->last_block_ends_at = lbe;
-        st->rotations = rotations;
-        st->min_from = min_from;
-        st->max_to = max_to;
-        st->max_thickness = kmax;
-        st->total_rotations += rotations;
-        st->early_flushes += early;
+    if (warp == 0) {
+        int32_t kmax = 0;
+        for (int64_t q = lane; q < n; q += 32) kmax = max(kmax, place[q]);
+        kmax = warp_max(kmax);
+        if (lane == 0) {
+            if (status == CHASE_RUNNING) status = did ? CHASE_FLUSH : CHASE_CONVERGED;
+            st->status = status;
+            st->iter = iter;
+            st->last_block_ends_at = lbe;
+            st->rotations = rotations;
+            st->min_from = min_from;
+            st->max_to = max_to;
+            st->max_thickness = kmax;
+            st->total_rotations += rotations;
+            st->early_flushes += early;
+        }
     }
 }
-
 
 // ---- batched chase: one lane per matrix --------------------------------------------------
 //
@@ -402,7 +626,7 @@ chase_batched_kernel(const BatchMat* __restrict__ mats, const int32_t* __restric
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
                          int32_t* place, cudaStream_t stream)
 {
-    chase_kernel<<<1, 32, 0, stream>>>(state, d, e, grid, thick, place);
+    chase_kernel<<<1, 64, 0, stream>>>(state, d, e, grid, thick, place);
     return cudaGetLastError();
 }
 

@@ -72,6 +72,7 @@ struct ChaseState {
     int64_t max_thickness;       // thickest column of the rotation grid (placement layers)
     int64_t total_rotations;
     int64_t early_flushes;       // flushes ended because a sweep's layer exceeded grid_layers
+    double  neg_zero;            // -0.0, supplied at run time (see mulz in chase.cu)
 };
 
 // ---- launch helpers (defined in the .cu files) ------------------------------------------
