@@ -19,6 +19,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -47,6 +48,13 @@ def parse_args():
     p.add_argument("--n", type=int, default=16384)
     p.add_argument("--k", type=int, default=64)
     p.add_argument("--no-extras", action="store_true", help="skip the FP32 and n=2000 side measurements")
+    p.add_argument("--workload", choices=["apply", "solve"], default="apply",
+                   help="apply: the bulk-apply microbenchmark (default); solve: one full qr_algorithm!")
+    p.add_argument("--case", choices=["A", "B"], default="A",
+                   help="solve workload: A d_i = i, e ~ U[0,1) (seed 1); B d ~ N(0,1), e ~ 0.5 N(0,1) (seed 2)")
+    p.add_argument("--q", choices=["f64", "f32"], default="f64", help="solve workload: Q precision")
+    p.add_argument("--oracle-check", action="store_true",
+                   help="solve workload: also run the CPU oracle's chase (eigenvalues only) and compare bits")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -371,10 +379,88 @@ def side_measurements(pkg, lib, h, dev, stream, args):
     return out
 
 
+def solve_inputs(n, case):
+    if case == "A":
+        rng = np.random.default_rng(1)
+        return np.arange(1, n + 1, dtype=np.float64), rng.random(n - 1)
+    rng = np.random.default_rng(2)
+    return rng.standard_normal(n), 0.5 * rng.standard_normal(n - 1)
+
+
+def run_solve(args):
+    """One full qr_algorithm!(SymTridiagonal(d, e), Q = I) on the device (the full-eigensolve
+    workload: n = 16384, case A or B, FP64 or FP32 Q), with its errors stated: eigenvalues
+    against LAPACK (scipy stemr) and, optionally, bit-for-bit against the CPU oracle's chase;
+    ||TQ - QD||_F / ||T||_F and ||Q^T Q - I||_F computed on the GPU in FP64."""
+    import torch
+    import __graft_entry__ as ge
+    from scipy.linalg import eigh_tridiagonal
+    pkg = ge.load_package()
+    n = args.n
+    d, e = solve_inputs(n, args.case)
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    qdt = torch.float64 if args.q == "f64" else torch.float32
+    h = pkg.Handle(0)
+    td, te = torch.from_numpy(d.copy()).to(dev), torch.from_numpy(e.copy()).to(dev)
+    Q = torch.eye(n, dtype=qdt, device=dev).T
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        _, conv, it = pkg.qr_algorithm_(pkg.SymTridiagonal(td, te), Q, handle=h)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+    st = h.stats()
+    lam = td.cpu().numpy()
+    # errors in FP64 on the GPU: T Q via the tridiagonal product, Q^T Q - I by GEMM
+    Q64 = Q.to(torch.float64)
+    dT, eT = torch.from_numpy(d).to(dev), torch.from_numpy(e).to(dev)
+    TQ = dT[:, None] * Q64
+    TQ[:-1] += eT[:, None] * Q64[1:]
+    TQ[1:] += eT[:, None] * Q64[:-1]
+    resid = float(torch.linalg.norm(TQ - Q64 * td[None, :]) / math.sqrt(float((d * d).sum() + 2 * (e * e).sum())))
+    del TQ
+    G = Q64.T @ Q64
+    G.diagonal().sub_(1.0)
+    orth = float(torch.linalg.norm(G))
+    del G, Q64
+    ref = eigh_tridiagonal(d, e, eigvals_only=True)
+    normT = float(np.max(np.abs(ref)))
+    eig_err = float(np.max(np.abs(np.sort(lam) - ref)))
+    eps = float(np.finfo(np.float64).eps)
+    out = {
+        "metric": f"qr_algorithm! full solve seconds, n={n} case {args.case}, Q {args.q}",
+        "value": round(secs, 3), "unit": "s", "higher_is_better": False, "n_gpus": 1,
+        "dtype": "f64" if args.q == "f64" else "f64 chase, f32 Q",
+        "data": "synthetic (seeded, as in the full-eigensolve configuration)",
+        "config": {"workload": "qr_algorithm!(SymTridiagonal(d, e), Q = I)", "n": n, "case": args.case,
+                   "q": args.q, "max_layers": 128},
+        "converged": bool(conv), "iterations": it, "rotations": st["rotations"], "flushes": st["flushes"],
+        "chase_ms": round(st["chase_ms"], 1), "apply_ms": round(st["apply_ms"], 1),
+        "chase_us_per_rotation": round(st["chase_ms"] * 1e3 / max(st["rotations"], 1), 4),
+        "givens_gflops_apply": round(6.0 * n * st["rotations"] / (st["apply_ms"] * 1e-3) / 1e9, 1),
+        "early_flushes": st["early_flushes"],
+        "errors": {"eig_max_abs_vs_lapack": eig_err, "eig_bound_10n_eps_normT": 10 * n * eps * normT,
+                   "resid_rel": resid, "orth": orth, "bound_10n_eps": 10 * n * eps},
+        "clocks": clk.summary(),
+    }
+    if args.oracle_check:
+        from oracle import oracle as orc
+        od, oe = d.copy(), e.copy()
+        t0 = time.perf_counter()
+        c_o, it_o, fl_o, rot_o = orc.qr_algorithm(od, oe, None)
+        out["oracle_chase"] = {"seconds_1_core": round(time.perf_counter() - t0, 2), "iterations": it_o,
+                               "eigenvalues_bit_equal": bool(np.array_equal(od, lam))}
+    print(json.dumps(out), flush=True)
+    h.close()
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "solve":
+        run_solve(args)
     else:
         run_ours(args)
 

@@ -150,6 +150,11 @@ int symeig_qr_batched_f64_dev(symeig_handle h, int64_t count, const int64_t* n, 
  * of each size class (n <= split, n > split) and keeps the faster one per class, process-wide.
  * ms (may be NULL) receives 4 timings [class][shape].  No reference counterpart. */
 int symeig_batched_autotune(symeig_handle h, double* ms);
+/* Read (set = 0) or write (set != 0) the tile shape of the single-matrix wave kernel for FP64
+ * (fp64 != 0) or FP32: 0 = 8 lane groups of 8 layers (4 rows per warp), 1 = 4 groups of 16
+ * layers (8 rows per warp).  Defaults: FP64 0, FP32 1.  Process-wide.  No reference
+ * counterpart. */
+int symeig_apply_tuning(int32_t fp64, int32_t* shape, int32_t set);
 /* Read (set = 0) or write (set != 0) the batched tuning: class split and shape per class. */
 int symeig_batched_tuning(int64_t* split, int32_t* shape_small, int32_t* shape_large, int32_t set);
 
@@ -187,6 +192,21 @@ int symeig_eig_adjoint_f64_dev(symeig_handle h, int64_t count, int64_t n, const 
 #define SYMEIG_NOALLOC_SCRATCH_BYTES (32u << 20)
 int symeig_apply_givens_f64_noalloc(double* A, int64_t lda, int64_t m, int64_t n,
                                     const double* cs, int64_t k, void* stream);
+
+/* ---- bulk lmul!: row rotations  (src/simple_givens.jl:38-51) --------------------------------- *
+ * A (m x n, column-major, lda >= m) <- prod of the (m-1) x k grid of row rotations cs applied
+ * from the left, in layer-major order: for L in 1:k, for i in 1:m-1, lmul!(G[i,L], A)
+ * (rows i, i+1: a_i <- c a_i + s a_{i+1}, a_{i+1} <- -s a_i + c a_{i+1}).  The reference has
+ * only the single-rotation lmul!; this is its bulk form (e.g. for applying Q^T to a block of
+ * vectors).  Same cs layout as symeig_apply_givens_* with m in place of n. */
+int symeig_apply_givens_left_f64(symeig_handle h, double* A, int64_t lda, int64_t m, int64_t n,
+                                 const double* cs, int64_t k);
+int symeig_apply_givens_left_f32(symeig_handle h, float* A, int64_t lda, int64_t m, int64_t n,
+                                 const float* cs, int64_t k);
+int symeig_apply_givens_left_f64_dev(symeig_handle h, double* A, int64_t lda, int64_t m,
+                                     int64_t n, const double* cs, int64_t k);
+int symeig_apply_givens_left_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t m,
+                                     int64_t n, const float* cs, int64_t k);
 
 /* ---- eigen_decomp!  (src/bulge_chasing.jl:290-299) ----------------------------------- *
  * Q (n x n, ldq >= n) is set to the identity, then qr_algorithm! runs with the default

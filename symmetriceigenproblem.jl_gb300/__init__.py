@@ -7,6 +7,7 @@ loads it by path (see ``__graft_entry__.load_package``).
 """
 from .api import (  # noqa: F401
     SymTridiagonal,
+    bulk_wave_order_2x2_lmul_,
     bulk_wave_order_2x2_rmul_,
     bulk_wave_order_2x2_rmul_parallel_,
     eig_adjoint,

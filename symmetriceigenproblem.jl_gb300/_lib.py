@@ -44,11 +44,16 @@ SIGNATURES = {
     "symeig_apply_givens_f32": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
     "symeig_apply_givens_f64_dev": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
     "symeig_apply_givens_f32_dev": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
+    "symeig_apply_givens_left_f64": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
+    "symeig_apply_givens_left_f32": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
+    "symeig_apply_givens_left_f64_dev": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
+    "symeig_apply_givens_left_f32_dev": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
     "symeig_apply_givens_f64_noalloc": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp]),
     "symeig_qr_batched_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_dbl, c_i64, c_vp, c_vp]),
     "symeig_qr_batched_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_dbl, c_i64, c_vp, c_vp]),
     "symeig_batched_autotune": (ctypes.c_int, [c_vp, c_vp]),
     "symeig_batched_tuning": (ctypes.c_int, [P_i64, P_i32, P_i32, c_i32]),
+    "symeig_apply_tuning": (ctypes.c_int, [c_i32, P_i32, c_i32]),
     "symeig_eig_adjoint_f64": (ctypes.c_int, [c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "symeig_eig_adjoint_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "symeig_eigen_decomp_f64": (ctypes.c_int, [c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, P_i32, P_i64]),

@@ -118,13 +118,13 @@ def _givens_ptr(givens, dtype_name: str, on_device: bool):
 def bulk_wave_order_2x2_rmul_(A, givens, handle: Handle | None = None) -> None:
     """A <- A * prod(G) for the (n-1) x k rotation grid, in the reference's wave order
     (src/wave.jl:62-162).  Unlike the reference, any n and any k are accepted."""
-    h = handle or default_handle(A.device.index if _is_torch(A) else 0)
     ptr, ld, m, n, dt, dev = _colmajor_info(A)
     gn = int(givens.shape[0])
     if n >= 2 and gn != n - 1:
         raise ValueError(f"givens has {gn} rows, expected n-1 = {n - 1}")
     if n < 2 or m == 0 or int(givens.shape[1]) == 0:
         return None
+    h = handle or default_handle(A.device.index if _is_torch(A) else 0)
     gptr, keep, k = _givens_ptr(givens, dt, dev)
     name = f"symeig_apply_givens_{dt}" + ("_dev" if dev else "")
     if dev:  # run on torch's current stream: ordered after the producers of A and givens
@@ -353,3 +353,27 @@ if torch is not None:
             if glam is None:
                 glam = torch.zeros_like(lam)
             return eig_adjoint(lam, Q, glam.contiguous(), gQ)
+
+
+def bulk_wave_order_2x2_lmul_(A, givens, handle: Handle | None = None) -> None:
+    """A <- (row rotations) * A: the bulk form of lmul!(G, A) (src/simple_givens.jl:38-51) for an
+    (m-1) x k grid, layer-major (for L, for i: rows i, i+1).  The reference has only the
+    single-rotation lmul!.  Same array conventions as bulk_wave_order_2x2_rmul_, with givens of
+    shape (m-1, k, 2)."""
+    ptr, ld, m, n, dt, dev = _colmajor_info(A)
+    gm = int(givens.shape[0])
+    if m >= 2 and gm != m - 1:
+        raise ValueError(f"givens has {gm} rows, expected m-1 = {m - 1}")
+    if m < 2 or n == 0 or int(givens.shape[1]) == 0:
+        return None
+    h = handle or default_handle(A.device.index if _is_torch(A) else 0)
+    gptr, keep, k = _givens_ptr(givens, dt, dev)
+    name = f"symeig_apply_givens_left_{dt}" + ("_dev" if dev else "")
+    if dev:
+        with h.on_stream(torch.cuda.current_stream(A.device).cuda_stream):
+            h.call(name, ctypes.c_void_p(ptr), ld, m, n, ctypes.c_void_p(gptr), k)
+        torch.cuda.current_stream(A.device).synchronize()
+    else:
+        h.call(name, ctypes.c_void_p(ptr), ld, m, n, ctypes.c_void_p(gptr), k)
+    del keep
+    return None

@@ -3,16 +3,17 @@
 //
 // qr driver.  The reference's outer loop (src/bulge_chasing.jl:166-284) alternates a serial
 // chase that fills a (n-1) x max_layers rotation buffer with a bulk application of that
-// buffer to Q.  Here the chase is a one-warp kernel on a side stream and the apply is the
-// wave-window kernel on the main stream.  The rotation grid is double-buffered: the chase of
-// flush f+1 runs while flush f is applied, since the chase reads only (d, e) and the apply
-// reads only the grid and Q.  After each chase the host reads its 100-byte status (pinned
-// memory) to learn whether to apply, stop (converged) or give up (maxiter), exactly the
-// three exits of the reference.
+// buffer to Q.  Here the chase is a two-warp kernel on a side stream and the apply is the
+// wave-window kernel on the main stream, ordered by events: chase f, apply f, chase f+1, ...
+// (the rotation grid is double-buffered so that a concurrent schedule is possible; see the
+// note in the flush loop for why it is not used).  After each chase the host reads its
+// status (pinned memory) to learn whether to apply, stop (converged) or give up (maxiter),
+// exactly the three exits of the reference.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <chrono>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -134,13 +135,14 @@ void begin_call(symeig_handle h)
 // Run every pass of one bulk apply of `layers` layers of `grid` to columns [c0, c0+n_loc).
 template <typename Tsrc, typename T>
 int apply_grid(symeig_handle h, T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t grid_rows,
-               const int32_t* thick, int64_t c0, int64_t n_loc, int64_t layers, cudaStream_t s)
+               const int32_t* thick, int64_t c0, int64_t n_loc, int64_t layers, cudaStream_t s,
+               int64_t rs = 1)
 {
     if (m <= 0 || n_loc < 2 || layers <= 0) return SYMEIG_OK;
     const int64_t per = apply_layers_per_pass<T>();
     CK(h->table.ensure(apply_table_bytes<T>(n_loc, per)));
     for (int64_t L0 = 0; L0 < layers; L0 += per) {
-        ApplyPass pass{c0, n_loc, L0, std::min(per, layers - L0)};
+        ApplyPass pass{c0, n_loc, L0, std::min(per, layers - L0), rs};
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (h->kernel_timing) {
             e0 = kernel_event(h);
@@ -206,6 +208,8 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     // the memcpy above reads a stack object: make it complete before returning from scope
     CK(cudaStreamSynchronize(cs));
 
+    // SYMEIG_DEBUG=1 prints one line per flush to stderr.
+    static const bool debug = std::getenv("SYMEIG_DEBUG") != nullptr;
     size_t tev = 0;
     double chase_ms = 0.0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> apply_marks;
@@ -214,7 +218,11 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     int result = SYMEIG_OK;
     for (;; ++flush) {
         const int b = (int)(flush & 1);
-        if (flush >= 2) CK(cudaStreamWaitEvent(cs, h->ev_consumed[b], 0));
+        // The chase of a flush starts after the previous flush's apply has finished.  Running
+        // them concurrently (they touch disjoint buffers) was tried: at n = 8192 a chase that
+        // overlapped a 512-CTA apply did not finish within 150 s, for a reason not yet found,
+        // so the two are serialised.  The apply is ~5% of the chase time at these sizes.
+        if (flush >= 1) CK(cudaStreamWaitEvent(cs, h->ev_consumed[b ^ 1], 0));
         cudaEvent_t c0 = timing_event(h, tev++), c1 = timing_event(h, tev++);
         if (!c0 || !c1) return SYMEIG_ERR_CUDA;
         CK(cudaEventRecord(c0, cs));
@@ -228,6 +236,11 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
         CK(cudaEventElapsedTime(&ms_chase, c0, c1));
         chase_ms += ms_chase;
         const ChaseState st = *h->h_state;
+        if (debug)
+            fprintf(stderr, "[symeig] flush %lld: chase %.1f ms status %d rot %lld K %lld cols %lld..%lld t=%.1f ms\n",
+                    (long long)flush, ms_chase, st.status, (long long)st.rotations,
+                    (long long)st.max_thickness, (long long)st.min_from, (long long)st.max_to,
+                    std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count());
         if (st.status == CHASE_MAXITER) { conv = 0; break; }
         if (st.status == CHASE_CONVERGED) break;
         if (st.status != CHASE_FLUSH) { result = SYMEIG_ERR_DEVICE; break; }
@@ -355,9 +368,77 @@ int apply_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T
     return SYMEIG_OK;
 }
 
+// Row rotations (lmul!, src/simple_givens.jl:38-51) of an m x n column-major A: the wave
+// kernel on the transposed view, whose rows (A's columns) are lda apart and whose columns
+// (A's rows) are adjacent.  The grid is (m-1) x k.
+template <typename T>
+int apply_left_dev(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T* cs, int64_t k)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (k < 0 || m < 0) return SYMEIG_ERR_SIZE;
+    rc = validate_matrix(A, lda, m, n);
+    if (rc) return rc;
+    if (m > ((int64_t)1 << 30)) return SYMEIG_ERR_SIZE;
+    if (m >= 2 && k > 0 && !cs) return SYMEIG_ERR_NULL;
+    begin_call(h);
+    if (n == 0 || m < 2 || k == 0) return SYMEIG_OK;
+    return apply_grid<T, T>(h, A, 1, n, cs, m - 1, nullptr, 0, m, k, h->stream, lda);
+}
+
+template <typename T>
+int apply_left_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T* cs, int64_t k)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (k < 0 || m < 0) return SYMEIG_ERR_SIZE;
+    rc = validate_matrix(A, lda, m, n);
+    if (rc) return rc;
+    if (m >= 2 && k > 0 && !cs) return SYMEIG_ERR_NULL;
+    if (n == 0 || m < 2 || k == 0) return SYMEIG_OK;
+    cudaStream_t s = h->stream;
+    CK(h->q.ensure((size_t)m * n * sizeof(T)));
+    const size_t cs_bytes = (size_t)(m - 1) * k * 2 * sizeof(T);
+    CK(h->cs.ensure(cs_bytes));
+    CK(cudaMemcpyAsync(h->cs.ptr, cs, cs_bytes, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpy2DAsync(h->q.ptr, m * sizeof(T), A, lda * sizeof(T), m * sizeof(T), n,
+                         cudaMemcpyHostToDevice, s));
+    rc = apply_left_dev<T>(h, (T*)h->q.ptr, m, m, n, (const T*)h->cs.ptr, k);
+    if (rc) return rc;
+    CK(cudaMemcpy2DAsync(A, lda * sizeof(T), h->q.ptr, m * sizeof(T), m * sizeof(T), n,
+                         cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return SYMEIG_OK;
+}
+
 }  // namespace
 
 extern "C" {
+
+int symeig_apply_givens_left_f64(symeig_handle h, double* A, int64_t lda, int64_t m, int64_t n,
+                                 const double* cs, int64_t k)
+{
+    return apply_left_host<double>(h, A, lda, m, n, cs, k);
+}
+
+int symeig_apply_givens_left_f32(symeig_handle h, float* A, int64_t lda, int64_t m, int64_t n,
+                                 const float* cs, int64_t k)
+{
+    return apply_left_host<float>(h, A, lda, m, n, cs, k);
+}
+
+int symeig_apply_givens_left_f64_dev(symeig_handle h, double* A, int64_t lda, int64_t m,
+                                     int64_t n, const double* cs, int64_t k)
+{
+    return apply_left_dev<double>(h, A, lda, m, n, cs, k);
+}
+
+int symeig_apply_givens_left_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t m,
+                                     int64_t n, const float* cs, int64_t k)
+{
+    return apply_left_dev<float>(h, A, lda, m, n, cs, k);
+}
+
 
 int symeig_create(symeig_handle* out, int device)
 {
@@ -608,6 +689,18 @@ int symeig_qr_batched_f64(symeig_handle h, int64_t count, const int64_t* n, doub
     CK(cudaStreamSynchronize(s));
     h->stats.total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return SYMEIG_OK;
+}
+
+int symeig_apply_tuning(int32_t fp64, int32_t* shape, int32_t set)
+{
+    if (!shape) return SYMEIG_ERR_NULL;
+    if (set) {
+        if (*shape < 0 || *shape > 1) return SYMEIG_ERR_SIZE;
+        apply_set_shape(fp64, *shape);
+    } else {
+        *shape = apply_get_shape(fp64);
+    }
     return SYMEIG_OK;
 }
 

@@ -109,6 +109,21 @@ __device__ __forceinline__ void givens(double f, double g, double& cs, double& s
     }
 }
 
+// givensAlgorithm with its branch tests on the integer pipe and its products issued as FMAs
+// (same results as givens()); the rare branches fall back to givens().
+__device__ __forceinline__ void givens_fast(double f, double g, double& cs, double& sn, double& r,
+                                            double nz)
+{
+    if (givens_case(f, g) != 4) {
+        givens(f, g, cs, sn, r);
+        return;
+    }
+    r = __dsqrt_rn(__dadd_rn(mulz(f, f, nz), mulz(g, g, nz)));
+    cs = __ddiv_rn(f, r);
+    sn = __ddiv_rn(g, r);
+    if (givens_flip(f, g, cs)) { cs = neg(cs); sn = neg(sn); r = neg(r); }
+}
+
 // is_offdiagonal_small(H, j, tol), 1-based j (src/bulge_chasing.jl:7-8).
 __device__ __forceinline__ bool is_small(const double* dv, const double* ev, int64_t j, double tol)
 {
@@ -130,10 +145,16 @@ __device__ __forceinline__ double wilkinson_shift(double a, double b, double c)
     return __dmul_rn(lam, scale);
 }
 
-__device__ __forceinline__ double fsum(double u, double a, double v, double b)
+__device__ __forceinline__ double fsum(double u, double a, double v, double b, double nz)
 {
     // u*a + v*b with the first product fused
-    return __fma_rn(u, a, __dmul_rn(v, b));
+    return __fma_rn(u, a, mulz(v, b, nz));
+}
+
+// u*a - v*b with the first product fused
+__device__ __forceinline__ double fdif(double u, double a, double v, double b, double nz)
+{
+    return __fma_rn(u, a, neg(mulz(v, b, nz)));
 }
 
 // Record (c,s) of rotation i (1-based).  thick[i] is the reference's layer_thickness (it
@@ -157,18 +178,18 @@ __device__ __forceinline__ void record(double* grid, int32_t* thick, int32_t* pl
 __device__ void single_shift(double* __restrict__ dv, double* __restrict__ ev, int64_t from,
                              int64_t to, double mu, double* __restrict__ grid,
                              int32_t* __restrict__ thick, int32_t* __restrict__ place,
-                             int64_t rows, int32_t layer)
+                             int64_t rows, int32_t layer, double nz)
 {
     const double H11 = dv[from - 1], H21 = ev[from - 1], H22 = dv[from];
     double c, s, nrm;
-    givens(__dsub_rn(H11, mu), H21, c, s, nrm);
-    const double H11p = fsum(c, H11, s, H21);
-    const double H21p = __fma_rn(c, H21, -__dmul_rn(s, H11));
-    const double H12p = fsum(c, H21, s, H22);
-    const double H22p = __fma_rn(c, H22, -__dmul_rn(s, H21));
-    const double H11pp = fsum(H11p, c, H12p, s);
-    const double H12pp = __fma_rn(H12p, c, -__dmul_rn(H11p, s));
-    const double H22pp = __fma_rn(H22p, c, -__dmul_rn(H21p, s));
+    givens_fast(__dsub_rn(H11, mu), H21, c, s, nrm, nz);
+    const double H11p = fsum(c, H11, s, H21, nz);
+    const double H21p = fdif(c, H21, s, H11, nz);
+    const double H12p = fsum(c, H21, s, H22, nz);
+    const double H22p = fdif(c, H22, s, H21, nz);
+    const double H11pp = fsum(H11p, c, H12p, s, nz);
+    const double H12pp = fdif(H12p, c, H11p, s, nz);
+    const double H22pp = fdif(H22p, c, H21p, s, nz);
     dv[from - 1] = H11pp;
     dv[from] = H22pp;
     ev[from - 1] = H12pp;
@@ -176,8 +197,8 @@ __device__ void single_shift(double* __restrict__ dv, double* __restrict__ ev, i
     double e_next = 0.0;  // ev[i] (1-based) entering step i
     if (from + 2 <= to) {
         const double H23 = ev[from];
-        bulge = __dmul_rn(s, H23);
-        e_next = __dmul_rn(c, H23);
+        bulge = mulz(s, H23, nz);
+        e_next = mulz(c, H23, nz);
         ev[from] = e_next;
     }
     record(grid, thick, place, rows, from, layer, c, s);
@@ -192,22 +213,22 @@ __device__ void single_shift(double* __restrict__ dv, double* __restrict__ ev, i
         // prefetch for step i+1: dv[i+2], ev[i+2] (1-based)
         if (i + 1 <= to - 1) B22_n = dv[i + 1];
         if (i + 3 <= to) B23_n = ev[i + 1];
-        givens(p1, bulge, c, s, nrm);
+        givens_fast(p1, bulge, c, s, nrm, nz);
         ev[i - 2] = nrm;
         const double B21 = e_next;
-        const double B11p = fsum(c, B11, s, B21);
-        const double B21p = __fma_rn(c, B21, -__dmul_rn(s, B11));
-        const double B12p = fsum(c, B21, s, B22);
-        const double B22p = __fma_rn(c, B22, -__dmul_rn(s, B21));
-        const double B11pp = fsum(B11p, c, B12p, s);
-        const double B12pp = __fma_rn(B12p, c, -__dmul_rn(B11p, s));
-        const double B22pp = __fma_rn(B22p, c, -__dmul_rn(B21p, s));
+        const double B11p = fsum(c, B11, s, B21, nz);
+        const double B21p = fdif(c, B21, s, B11, nz);
+        const double B12p = fsum(c, B21, s, B22, nz);
+        const double B22p = fdif(c, B22, s, B21, nz);
+        const double B11pp = fsum(B11p, c, B12p, s, nz);
+        const double B12pp = fdif(B12p, c, B11p, s, nz);
+        const double B22pp = fdif(B22p, c, B21p, s, nz);
         dv[i - 1] = B11pp;
         dv[i] = B22pp;
         ev[i - 1] = B12pp;
         if (i + 2 <= to) {
-            bulge = __dmul_rn(s, B23);
-            e_next = __dmul_rn(c, B23);
+            bulge = mulz(s, B23, nz);
+            e_next = mulz(c, B23, nz);
             ev[i] = e_next;
         }
         record(grid, thick, place, rows, i, layer, c, s);
@@ -581,7 +602,7 @@ __device__ void chase_flush_lane(ChaseState* __restrict__ st, double* __restrict
                         }
                 }
                 const double mu = wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
-                single_shift(dv, ev, from, to, mu, grid, thick, place, rows, layer);
+                single_shift(dv, ev, from, to, mu, grid, thick, place, rows, layer, st->neg_zero);
                 did = true;
                 iter += 1;
                 rotations += to - from;

@@ -80,6 +80,7 @@ struct ChaseState {
 // layers [L0, L0 + layers) of the (n-1) x * rotation grid.
 struct ApplyPass {
     int64_t c0, n_loc, L0, layers;
+    int64_t rs = 1;  // stride between the kernel's rows (1: rmul!, lda: lmul! on the transpose)
 };
 
 // Layers one pass of the wave-window kernel handles for element type T.
@@ -101,6 +102,10 @@ cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t g
                        const int32_t* thick, const ApplyPass& pass, void* table, int* err,
                        cudaStream_t stream, cudaEvent_t ev_begin = nullptr,
                        cudaEvent_t ev_end = nullptr);
+
+// Tile shape of the single-matrix wave kernel per precision (see apply.cu).
+void apply_set_shape(int fp64, int shape);
+int apply_get_shape(int fp64);
 
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
                          int32_t* place, cudaStream_t stream);

@@ -185,13 +185,16 @@ __device__ __forceinline__ void staging_init(Staging<Sh>& st)
     __syncthreads();
 }
 
-// One tile: rows [row0, row0 + ROWS) of Q (m rows, leading dimension ldq, columns
-// [0, n_loc) of the pass) through the n_chunks chunks of `table`.  Every thread of the CTA
-// calls it.  Returns false (all threads) when a bounded wait gave up.
+// One tile: rows [row0, row0 + ROWS) of Q (m rows, columns [0, n_loc) of the pass) through
+// the n_chunks chunks of `table`.  Element (row, col) is Q[row * rs + col * ldq]: rs = 1 for
+// the column rotations of rmul! on a column-major matrix, rs = lda and ldq = 1 for the row
+// rotations of lmul! (the same wave on the transposed view).  Every thread of the CTA calls
+// it.  Returns false (all threads) when a bounded wait gave up.
 template <typename T, typename Sh>
 __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_t m, int64_t row0,
                                           int32_t n_loc, const unsigned char* __restrict__ table,
-                                          int32_t n_chunks, const T nz, Staging<Sh>& st)
+                                          int32_t n_chunks, const T nz, Staging<Sh>& st,
+                                          int64_t rs = 1)
 {
     constexpr int KB = Sh::KB, G = Sh::G, CH = Sh::CH, W = Sh::W, RPW = Sh::RPW;
     const int tid = threadIdx.x;
@@ -206,7 +209,7 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
     const int rl = lane - g * RPW;
     const int64_t row = row0 + (tid >> 5) * RPW + rl;
     const bool row_ok = row < m;
-    T* __restrict__ qrow = Q + (row_ok ? row : 0);
+    T* __restrict__ qrow = Q + (row_ok ? row : 0) * rs;
     const bool storer = (g == G - 1) && row_ok;  // group G-1 writes Q
     const int lag = g * W;                       // waves this group trails group 0
 
@@ -232,15 +235,19 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
         const bool interior = (t0 + W + CH <= n_loc) && (t0 - (G - 1) * W - KB >= 0) &&
                               (t0 - KB + CH <= n_loc);
         if (interior) {
+            const T* lp = ld_base;
+            T* sp = st_base;
 #pragma unroll
             for (int u = 0; u < CH; ++u) {
                 const T up = __shfl_up_sync(0xffffffffu, xout, RPW);
                 const T xin = (g == 0) ? ahead[u % W] : up;
-                ahead[u % W] = ld_base[(int64_t)u * ldq];
+                ahead[u % W] = *lp;
+                lp += ldq;
                 win[u % W] = xin;
                 wave_rotations<T, KB>(win, sb + u * Sh::ITER, u % W, nz);
                 xout = win[(u + 1) % W];
-                st_pred(st_base + (int64_t)u * ldq, xout, storer);
+                if (storer) *sp = xout;
+                sp += ldq;
             }
         } else {
             const int32_t ld_cnt = min(max(n_loc - t0 - W, 0), CH);

@@ -10,6 +10,13 @@ eigensolver hot path.  The functions keep the reference's names and signatures:
     bulk_wave_order_2x2_rmul_parallel!(A, givens)              # src/wave.jl:36
     eigen_decomp!(H) -> (Diagonal(H.dv), Q)                    # src/bulge_chasing.jl:290
 
+and three additions without a reference counterpart:
+
+    qr_algorithm_batched!(Hs::Vector{SymTridiagonal{Float64}}, Qs; max_layers, tol, maxiter_factor)
+    tridiag_eigen(d, e) -> (lam, Q), differentiable through a ChainRulesCore rrule whose
+        pullback is the library's adjoint (FP64 tensor-core GEMMs with fused epilogues)
+    bulk_wave_order_2x2_lmul!(A, givens)                      # bulk form of lmul!, src/simple_givens.jl:38
+
 Q may be Matrix{Float64} or Matrix{Float32} (the FP32-Q variant: FP64 chase, (c,s) rounded to
 Float32).  Host arrays are copied to the GPU and back by the library.  Nothing is exported,
 as in the reference.  Unlike the reference, odd n is accepted.
@@ -17,6 +24,7 @@ as in the reference.  Unlike the reference, odd n is accepted.
 module SymmetricEigenProblemGB300
 
 using LinearAlgebra: SymTridiagonal, Diagonal, I
+using ChainRulesCore: ChainRulesCore, NoTangent, AbstractZero, unthunk
 
 const libsymeig = get(ENV, "SYMEIG_LIB",
                       joinpath(@__DIR__, "..", "_build", "libsymeig.so"))
@@ -76,6 +84,70 @@ end
 
 # Every row of A has its own GPU thread: the threaded variant is the same call.
 bulk_wave_order_2x2_rmul_parallel!(A, givens) = bulk_wave_order_2x2_rmul!(A, givens)
+
+function bulk_wave_order_2x2_lmul!(A::StridedMatrix{T}, givens::Matrix{Tuple{T,T}}) where {T<:Union{Float64,Float32}}
+    m, n = size(A)
+    size(givens, 1) == m - 1 || throw(DimensionMismatch("givens must have m-1 rows"))
+    stride(A, 1) == 1 || throw(ArgumentError("A must have unit row stride"))
+    fn = T === Float64 ? :symeig_apply_givens_left_f64 : :symeig_apply_givens_left_f32
+    st = GC.@preserve A givens ccall((fn, libsymeig), Cint,
+        (Ptr{Cvoid}, Ptr{T}, Int64, Int64, Int64, Ptr{Tuple{T,T}}, Int64),
+        handle(), A, stride(A, 2), m, n, givens, size(givens, 2))
+    check(fn, st)
+    return nothing
+end
+
+"""Many qr_algorithm! calls in one: H_i and Q_i (n_i x n_i) updated in place."""
+function qr_algorithm_batched!(Hs::Vector{SymTridiagonal{Float64,Vector{Float64}}}, Qs::Vector{Matrix{Float64}};
+                               max_layers::Int = 128, tol = eps(Float64), maxiter_factor::Int = 100)
+    ns = Int64[size(H, 1) for H in Hs]
+    d = reduce(vcat, [H.dv for H in Hs])
+    e = reduce(vcat, [H.ev for H in Hs])
+    Q = reduce(vcat, [vec(Q) for Q in Qs])
+    conv = zeros(Int32, length(Hs))
+    iters = zeros(Int64, length(Hs))
+    st = ccall((:symeig_qr_batched_f64, libsymeig), Cint,
+        (Ptr{Cvoid}, Int64, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int32, Float64, Int64,
+         Ptr{Int32}, Ptr{Int64}),
+        handle(), length(Hs), ns, d, e, Q, max_layers, Float64(tol), maxiter_factor, conv, iters)
+    check(:symeig_qr_batched_f64, st)
+    od = oe = oq = 0
+    for (k, n) in enumerate(ns)
+        Hs[k].dv .= view(d, od+1:od+n); od += n
+        Hs[k].ev .= view(e, oe+1:oe+n-1); oe += n - 1
+        vec(Qs[k]) .= view(Q, oq+1:oq+n*n); oq += n * n
+    end
+    return Hs, conv .!= 0, iters
+end
+
+"""(lam, Q) of SymTridiagonal(d, e): lam unsorted (as H.dv), Q the eigenvectors."""
+function tridiag_eigen(d::AbstractVector{Float64}, e::AbstractVector{Float64})
+    n = length(d)
+    H = SymTridiagonal(collect(d), collect(e))
+    Q = Matrix{Float64}(I, n, n)
+    _, converged, _ = qr_algorithm!(H, Q)
+    converged || error("qr_algorithm! did not converge")
+    return H.dv, Q
+end
+
+function ChainRulesCore.rrule(::typeof(tridiag_eigen), d::AbstractVector{Float64}, e::AbstractVector{Float64})
+    lam, Q = tridiag_eigen(d, e)
+    n = length(d)
+    function tridiag_eigen_pullback(ybar)
+        glam_t, gQ_t = unthunk(ybar)
+        glam = glam_t isa AbstractZero ? zeros(n) : collect(Float64, unthunk(glam_t))
+        gQ = gQ_t isa AbstractZero ? nothing : Matrix{Float64}(unthunk(gQ_t))
+        gd = zeros(n)
+        ge = zeros(max(n - 1, 0))
+        st = GC.@preserve lam Q glam gQ ccall((:symeig_eig_adjoint_f64, libsymeig), Cint,
+            (Ptr{Cvoid}, Int64, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+             Ptr{Float64}, Ptr{Float64}),
+            handle(), 1, n, lam, Q, glam, gQ === nothing ? C_NULL : gQ, gd, ge)
+        check(:symeig_eig_adjoint_f64, st)
+        return NoTangent(), gd, ge
+    end
+    return (lam, Q), tridiag_eigen_pullback
+end
 
 function eigen_decomp!(H::SymTridiagonal{Float64})
     n = size(H, 1)

@@ -44,3 +44,45 @@ def test_apply_host_buffers_with_leading_dimension(cuda, pkg, oracle, dtype):
     pkg.bulk_wave_order_2x2_rmul_(A, g)
     assert np.array_equal(A, ref)
     assert np.array_equal(big[m:, :], untouched)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("m,n,k", [(2, 1, 1), (9, 5, 3), (65, 40, 64), (130, 33, 70)])
+def test_left_apply_matches_oracle(cuda, pkg, oracle, m, n, k, dtype):
+    """Bulk lmul! (row rotations) == the oracle's column rotations of the transpose."""
+    rng = np.random.default_rng(m + 7 * n + k)
+    g = rotation_grid(pkg, rng, m, k, dtype)          # (m-1) x k grid
+    A = np.asfortranarray((rng.random((m, n)) * 2 - 1).astype(dtype))
+    refT = np.asfortranarray(A.T.copy())
+    oracle.apply_seq(refT, g)
+    dA = to_device_colmajor(cuda, A)
+    pkg.bulk_wave_order_2x2_lmul_(dA, cuda.from_numpy(np.ascontiguousarray(g)).cuda())
+    assert np.array_equal(dA.cpu().numpy(), refT.T)
+    B = A.copy(order="F")
+    pkg.bulk_wave_order_2x2_lmul_(B, g)
+    assert np.array_equal(B, refT.T)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("shape", [0, 1])
+def test_apply_both_tile_shapes(cuda, pkg, oracle, dtype, shape):
+    """Both tile shapes of the single-matrix wave kernel give the oracle's bits."""
+    import ctypes
+    lib = pkg.load_library()
+    fp64 = int(dtype == np.float64)
+    old = ctypes.c_int32()
+    assert lib.symeig_apply_tuning(fp64, ctypes.byref(old), 0) == 0
+    v = ctypes.c_int32(shape)
+    assert lib.symeig_apply_tuning(fp64, ctypes.byref(v), 1) == 0
+    try:
+        rng = np.random.default_rng(99 + shape)
+        for (m, n, k) in [(33, 70, 64), (100, 129, 130), (7, 20, 5)]:
+            g = rotation_grid(pkg, rng, n, k, dtype)
+            A = np.asfortranarray((rng.random((m, n)) * 2 - 1).astype(dtype))
+            ref = A.copy(order="F")
+            oracle.apply_seq(ref, g)
+            dA = to_device_colmajor(cuda, A)
+            pkg.bulk_wave_order_2x2_rmul_(dA, cuda.from_numpy(np.ascontiguousarray(g)).cuda())
+            assert np.array_equal(dA.cpu().numpy(), ref)
+    finally:
+        assert lib.symeig_apply_tuning(fp64, ctypes.byref(old), 1) == 0

@@ -1,0 +1,104 @@
+"""Host-side logic of the Python mirror that needs no GPU: argument validation raises before
+any library call, layouts are recognised, and the packing helpers are consistent."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+
+def test_symtridiagonal_dense_and_copy(pkg):
+    H = pkg.SymTridiagonal(np.array([1.0, 2.0, 3.0]), np.array([0.5, -0.25]))
+    T = H.dense()
+    assert np.array_equal(T, np.array([[1, 0.5, 0], [0.5, 2, -0.25], [0, -0.25, 3.0]]))
+    H2 = H.copy()
+    H2.dv[0] = 9.0
+    assert H.dv[0] == 1.0 and H.n == 3
+
+
+def test_givens_buffer_is_julia_layout(pkg):
+    g = pkg.givens_buffer(5, 3)
+    assert g.shape == (5, 3, 2)
+    # pair, then i, then L: strides 8, 16, 16*(n-1) bytes
+    assert g.strides == (16, 80, 8)
+
+
+def test_row_major_matrix_is_rejected(pkg):
+    A = np.zeros((4, 5))                  # C order: not column-major
+    with pytest.raises(ValueError):
+        pkg.bulk_wave_order_2x2_rmul_(A, pkg.givens_buffer(4, 1))
+
+
+def test_apply_shape_mismatch_is_rejected(pkg):
+    A = np.asfortranarray(np.zeros((4, 5)))
+    with pytest.raises(ValueError):
+        pkg.bulk_wave_order_2x2_rmul_(A, pkg.givens_buffer(3, 1))   # needs n-1 = 4 rows
+    with pytest.raises(ValueError):
+        pkg.bulk_wave_order_2x2_lmul_(A, pkg.givens_buffer(4, 1))   # needs m-1 = 3 rows
+
+
+def test_qr_arguments_are_checked(pkg):
+    H = pkg.SymTridiagonal(np.zeros(4), np.zeros(2))         # ev must have n-1 entries
+    with pytest.raises(ValueError):
+        pkg.qr_algorithm_(H, None)
+    H = pkg.SymTridiagonal(np.zeros(4, dtype=np.float32), np.zeros(3, dtype=np.float32))
+    with pytest.raises(TypeError):
+        pkg.qr_algorithm_(H, None)
+    H = pkg.SymTridiagonal(np.zeros(4), np.zeros(3))
+    with pytest.raises(ValueError):
+        pkg.qr_algorithm_(H, np.asfortranarray(np.zeros((4, 3))))  # Q needs n columns
+
+
+def test_batched_packing_is_checked(pkg):
+    n = [3, 4]
+    with pytest.raises(ValueError):
+        pkg.qr_algorithm_batched_(np.zeros(6), np.zeros(5), n)      # d has sum(n) = 7
+    with pytest.raises(ValueError):
+        pkg.qr_algorithm_batched_(np.zeros(7), np.zeros(5), n, np.zeros(24))   # Q has 25
+    with pytest.raises(TypeError):
+        pkg.qr_algorithm_batched_(np.zeros(7, dtype=np.float32), np.zeros(5), n)
+
+
+def test_wave_port_threads_do_not_change_bits(oracle, pkg):
+    """The oracle's row-slab threading (src/wave.jl:44-57) gives the same bits for any count."""
+    rng = np.random.default_rng(4)
+    m, n, k = 100, 34, 8
+    th = rng.random((n - 1, k)) * 2 * np.pi
+    g = pkg.givens_buffer(n - 1, k)
+    g[..., 0], g[..., 1] = np.cos(th), np.sin(th)
+    A = np.asfortranarray(rng.random((m, n)))
+    outs = []
+    for t in (1, 2, 3, 7):
+        B = A.copy(order="F")
+        oracle.apply_wave(B, g, nthreads=t)
+        outs.append(B)
+    for B in outs[1:]:
+        assert np.array_equal(B, outs[0])
+
+
+def test_oracle_fp32_q_variant(oracle):
+    """FP32-Q oracle: the chase is FP64 (eigenvalues bit-equal to the FP64 run) and Q is the
+    FP32 product of the FP32-rounded rotations."""
+    rng = np.random.default_rng(8)
+    n = 50
+    d, e = rng.standard_normal(n), rng.random(n - 1)
+    d1, e1, d2, e2 = d.copy(), e.copy(), d.copy(), e.copy()
+    Q64 = np.asfortranarray(np.eye(n))
+    Q32 = np.asfortranarray(np.eye(n, dtype=np.float32))
+    oracle.qr_algorithm(d1, e1, Q64)
+    oracle.qr_algorithm(d2, e2, Q32)
+    assert np.array_equal(d1, d2)
+    assert np.max(np.abs(Q32.astype(np.float64) - Q64)) < 1e-4
+
+
+def test_oracle_flush_generator(oracle):
+    """qr_flushes walks the reference's outer loop: flushes with rotations, then converged."""
+    rng = np.random.default_rng(3)
+    n = 30
+    d, e = rng.standard_normal(n), rng.random(n - 1)
+    statuses = []
+    for rc, grid, thick, place, it in oracle.qr_flushes(d, e, max_layers=4):
+        statuses.append(rc)
+        if rc == 1:
+            assert thick.max() <= 4 and place.max() >= 1
+            assert grid.shape == (n - 1, 8, 2)   # exact-order grids hold 2 * max_layers
+    assert statuses[-1] == 0 and all(s == 1 for s in statuses[:-1]) and len(statuses) > 2
