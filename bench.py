@@ -55,6 +55,8 @@ def parse_args():
     p.add_argument("--q", choices=["f64", "f32"], default="f64", help="solve workload: Q precision")
     p.add_argument("--oracle-check", action="store_true",
                    help="solve workload: also run the CPU oracle's chase (eigenvalues only) and compare bits")
+    p.add_argument("--chase-mode", type=int, choices=[0, 1, 2], default=0,
+                   help="solve workload: 0 Newton-form two-warp chase, 1 reference form, 2 Newton + redo")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -407,7 +409,7 @@ def run_solve(args):
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         t0 = time.perf_counter()
-        _, conv, it = pkg.qr_algorithm_(pkg.SymTridiagonal(td, te), Q, handle=h)
+        _, conv, it = pkg.qr_algorithm_(pkg.SymTridiagonal(td, te), Q, handle=h, chase_mode=args.chase_mode)
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
     st = h.stats()
@@ -434,12 +436,12 @@ def run_solve(args):
         "dtype": "f64" if args.q == "f64" else "f64 chase, f32 Q",
         "data": "synthetic (seeded, as in the full-eigensolve configuration)",
         "config": {"workload": "qr_algorithm!(SymTridiagonal(d, e), Q = I)", "n": n, "case": args.case,
-                   "q": args.q, "max_layers": 128},
+                   "q": args.q, "max_layers": 128, "chase_mode": args.chase_mode},
         "converged": bool(conv), "iterations": it, "rotations": st["rotations"], "flushes": st["flushes"],
         "chase_ms": round(st["chase_ms"], 1), "apply_ms": round(st["apply_ms"], 1),
         "chase_us_per_rotation": round(st["chase_ms"] * 1e3 / max(st["rotations"], 1), 4),
         "givens_gflops_apply": round(6.0 * n * st["rotations"] / (st["apply_ms"] * 1e-3) / 1e9, 1),
-        "early_flushes": st["early_flushes"],
+        "early_flushes": st["early_flushes"], "redone_sweeps": st["redone_sweeps"],
         "errors": {"eig_max_abs_vs_lapack": eig_err, "eig_bound_10n_eps_normT": 10 * n * eps * normT,
                    "resid_rel": resid, "orth": orth, "bound_10n_eps": 10 * n * eps},
         "clocks": clk.summary(),

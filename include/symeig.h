@@ -51,6 +51,7 @@ typedef struct {
     int64_t wave_launches;   /* launches of the wave-window Givens kernel                 */
     double  wave_kernel_ms;  /* their summed device time (only with kernel timing on)     */
     int64_t device_errors;   /* nonzero if a kernel's bounded wait gave up (sticky)        */
+    int64_t redone_sweeps;   /* chase sweeps run again in the reference form (see below)  */
 } symeig_stats;
 
 /* Create a handle bound to CUDA device `device`.  Replaces nothing in the reference (the
@@ -70,6 +71,14 @@ int symeig_get_stats(symeig_handle h, symeig_stats* out);
  * 137-139), whose wave order differs from the chase's order when a split block re-merges
  * within a flush (Q then loses accuracy in the reference too).  No reference counterpart. */
 int symeig_set_exact_order(symeig_handle h, int32_t exact_order);
+/* How the chase kernel computes its rotations; every mode gives the same bits.
+ * 0 (default): two warps, givensAlgorithm's plain branch from FMA-only Newton steps whose
+ *   rounding is proved step by step; a sweep with an unproved step is restored and run again
+ *   in the reference form (counted in redone_sweeps).
+ * 1: the reference form (correctly rounded division and square root) on one thread.
+ * 2: as 0, but every sweep is then redone in the reference form (exercises the restore).
+ * No reference counterpart. */
+int symeig_set_chase_mode(symeig_handle h, int32_t mode);
 /* Record CUDA events around every wave-kernel launch so symeig_get_stats can report their
  * device time (wave_kernel_ms).  Off by default.  symeig_get_stats waits for the last
  * marked launch.  No reference counterpart (the reference times with BenchmarkTools). */

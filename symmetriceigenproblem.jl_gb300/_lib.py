@@ -32,6 +32,7 @@ SIGNATURES = {
     "symeig_get_stream": (ctypes.c_int, [c_vp, ctypes.POINTER(c_vp)]),
     "symeig_get_stats": (ctypes.c_int, [c_vp, c_vp]),
     "symeig_set_exact_order": (ctypes.c_int, [c_vp, c_i32]),
+    "symeig_set_chase_mode": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_kernel_timing": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, c_i32, ctypes.POINTER(c_dbl)]),
     "symeig_status_string": (ctypes.c_char_p, [ctypes.c_int]),
@@ -64,7 +65,7 @@ class Stats(ctypes.Structure):
     _fields_ = [("iterations", c_i64), ("flushes", c_i64), ("rotations", c_i64),
                 ("applied_rotation_rows", c_i64), ("chase_ms", c_dbl), ("apply_ms", c_dbl),
                 ("total_ms", c_dbl), ("early_flushes", c_i64), ("wave_launches", c_i64),
-                ("wave_kernel_ms", c_dbl), ("device_errors", c_i64)]
+                ("wave_kernel_ms", c_dbl), ("device_errors", c_i64), ("redone_sweeps", c_i64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -144,6 +145,11 @@ class Handle:
 
     def set_exact_order(self, exact: bool):
         check("symeig_set_exact_order", self._lib.symeig_set_exact_order(self.ptr, int(bool(exact))))
+
+    def set_chase_mode(self, mode):
+        """0: Newton-form two-warp chase (default); 1: reference form; 2: Newton form with
+        every sweep redone in the reference form.  All give the same bits."""
+        check("symeig_set_chase_mode", self._lib.symeig_set_chase_mode(self.ptr, int(mode)))
 
     def set_stream(self, stream_ptr: int | None):
         """Run *_dev calls on this cudaStream_t (0/None = the legacy default stream)."""

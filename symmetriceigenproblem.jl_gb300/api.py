@@ -147,13 +147,15 @@ def bulk_wave_order_2x2_rmul_parallel_(A, givens, handle: Handle | None = None) 
 
 def qr_algorithm_(H: SymTridiagonal, Q=None, max_layers: int = 128, tol: float | None = None,
                   maxiter: int | None = None, handle: Handle | None = None,
-                  exact_order: bool = True):
+                  exact_order: bool = True, chase_mode: int = 0):
     """qr_algorithm!(H, Q, max_layers=128, tol=eps(T), maxiter=100n) -> (H, converged, iter)
     (src/bulge_chasing.jl:146-288).  H.dv becomes the (unsorted) eigenvalues, Q <- Q*prod(G).
     Q may be None (eigenvalues only), float64 or float32 (the FP32-Q variant: FP64 chase,
     (c,s) rounded to float).  exact_order=False places rotations in the grid as the reference
     does (grid[i, ++layer_thickness[i]]), which loses accuracy in Q when a split block
-    re-merges within a flush; the default places each sweep at one layer so Q is exact."""
+    re-merges within a flush; the default places each sweep at one layer so Q is exact.
+    chase_mode selects how the chase computes rotations (symeig_set_chase_mode); every mode
+    gives the same bits."""
     n = H.n
     tol = EPS64 if tol is None else float(tol)
     maxiter = 100 * n if maxiter is None else int(maxiter)
@@ -183,6 +185,7 @@ def qr_algorithm_(H: SymTridiagonal, Q=None, max_layers: int = 128, tol: float |
     conv, it = c_i32(), c_i64()
     name = "symeig_qr_f64" + ("_q32" if dt == "f32" else "") + ("_dev" if dev else "")
     h.set_exact_order(exact_order)
+    h.set_chase_mode(chase_mode)
     try:
         args = (ctypes.c_void_p(dptr), ctypes.c_void_p(eptr), n, ctypes.c_void_p(qptr), ld, m,
                 int(max_layers), tol, maxiter, ctypes.byref(conv), ctypes.byref(it))
@@ -193,6 +196,7 @@ def qr_algorithm_(H: SymTridiagonal, Q=None, max_layers: int = 128, tol: float |
             h.call(name, *args)
     finally:
         h.set_exact_order(True)
+        h.set_chase_mode(0)
     return H, bool(conv.value), int(it.value)
 
 

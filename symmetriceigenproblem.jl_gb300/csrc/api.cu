@@ -54,9 +54,10 @@ struct symeig_context {
     cudaEvent_t ev_chased[2] = {nullptr, nullptr};
     cudaEvent_t ev_consumed[2] = {nullptr, nullptr};
     cudaEvent_t ev_main = nullptr;
-    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs;
+    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs, bak;
     int* derr = nullptr;   // device error word of the wave kernels (bounded waits)
     int32_t exact_order = 1;  // rotation placement of the qr driver
+    int32_t chase_mode = 0;   // symeig_set_chase_mode
     ChaseState* h_state = nullptr;  // pinned
     std::vector<cudaEvent_t> timing;  // pool of timing events
     symeig_stats stats{};
@@ -185,6 +186,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
         CK(h->place[b].ensure((size_t)n * sizeof(int32_t)));
     }
     CK(h->state.ensure(sizeof(ChaseState)));
+    CK(h->bak.ensure((size_t)2 * n * sizeof(double)));
 
     ChaseState init{};
     init.n = n;
@@ -198,6 +200,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     init.exact_order = h->exact_order;
     init.status = CHASE_RUNNING;
     init.neg_zero = -0.0;
+    init.chase_mode = h->chase_mode;
     ChaseState* dstate = (ChaseState*)h->state.ptr;
 
     cudaStream_t ms = h->stream, cs = h->chase_stream;
@@ -227,7 +230,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
         if (!c0 || !c1) return SYMEIG_ERR_CUDA;
         CK(cudaEventRecord(c0, cs));
         CK(launch_chase(dstate, d, e, (double*)h->grid[b].ptr, (int32_t*)h->thick[b].ptr,
-                        (int32_t*)h->place[b].ptr, cs));
+                        (int32_t*)h->place[b].ptr, (double*)h->bak.ptr, cs));
         CK(cudaEventRecord(c1, cs));
         CK(cudaMemcpyAsync(h->h_state, dstate, sizeof(ChaseState), cudaMemcpyDeviceToHost, cs));
         CK(cudaEventRecord(h->ev_chased[b], cs));
@@ -278,6 +281,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     h->stats.iterations = fin.iter;
     h->stats.rotations = fin.total_rotations;
     h->stats.early_flushes = fin.early_flushes;
+    h->stats.redone_sweeps = fin.redone_sweeps;
     h->stats.chase_ms = chase_ms;
     h->stats.apply_ms = apply_ms;
     h->stats.total_ms =
@@ -488,7 +492,7 @@ int symeig_destroy(symeig_handle h)
         if (h->ev_consumed[b]) cudaEventDestroy(h->ev_consumed[b]);
     }
     h->table.release(); h->state.release(); h->d.release(); h->e.release();
-    h->q.release(); h->cs.release();
+    h->q.release(); h->cs.release(); h->bak.release();
     if (h->ev_main) cudaEventDestroy(h->ev_main);
     for (cudaEvent_t ev : h->timing) cudaEventDestroy(ev);
     for (cudaEvent_t ev : h->kpool) cudaEventDestroy(ev);
@@ -520,6 +524,14 @@ int symeig_set_exact_order(symeig_handle h, int32_t exact_order)
 {
     if (!h) return SYMEIG_ERR_HANDLE;
     h->exact_order = exact_order ? 1 : 0;
+    return SYMEIG_OK;
+}
+
+int symeig_set_chase_mode(symeig_handle h, int32_t mode)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    if (mode < 0 || mode > 2) return SYMEIG_ERR_SIZE;
+    h->chase_mode = mode;
     return SYMEIG_OK;
 }
 

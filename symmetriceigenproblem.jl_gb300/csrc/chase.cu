@@ -19,110 +19,13 @@
 // The kernel never traps and never waits on another kernel: a flush ends by itself and
 // reports CHASE_FLUSH, CHASE_CONVERGED or CHASE_MAXITER in ChaseState.
 #include "symeig_common.cuh"
+#include "givens.cuh"
 
 namespace symeig {
 
 namespace {
 
-__device__ __forceinline__ double jl_max(double a, double b) { return (a > b || a != a) ? a : b; }
-
-// ---- bit-pattern tests on the integer pipe ----------------------------------------------
-// On GB300 every FP64 instruction, compares included, occupies the FP64 unit for ~64 cycles;
-// these give the same answers as the IEEE comparisons they replace.
-__device__ __forceinline__ uint64_t abs_bits(double x)
-{
-    return (uint64_t)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
-}
-__device__ __forceinline__ bool nan_bits(uint64_t a) { return a > 0x7FF0000000000000ull; }
-__device__ __forceinline__ double neg(double x)
-{
-    return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
-}
-// x < 0.0
-__device__ __forceinline__ bool is_negative(double x)
-{
-    const uint64_t b = (uint64_t)__double_as_longlong(x), a = b & 0x7FFFFFFFFFFFFFFFull;
-    return (b >> 63) != 0 && a != 0 && !nan_bits(a);
-}
-// a*b as an FMA with a -0.0 addend supplied at run time: bit-identical to the product, and an
-// FP64 FMA issues faster than an FP64 multiply on GB300.
-__device__ __forceinline__ double mulz(double a, double b, double nz) { return __fma_rn(a, b, nz); }
-
-// Which branch of givensAlgorithm (f, g) takes: 0 g == 0, 1 f == 0, 2 scaled down,
-// 3 scaled up, 4 plain (also when f or g is NaN: the NaN scale fails both range tests).
-__device__ __forceinline__ int givens_case(double f, double g)
-{
-    const uint64_t af = abs_bits(f), ag = abs_bits(g);
-    if (ag == 0) return 0;
-    if (af == 0) return 1;
-    if (nan_bits(af) || nan_bits(ag)) return 4;
-    const uint64_t m = af > ag ? af : ag;
-    if (m >= 0x5E40000000000000ull) return 2;  // max(|f|,|g|) >= 2^485
-    if (m <= 0x21A0000000000000ull) return 3;  // max(|f|,|g|) <= 2^-485
-    return 4;
-}
-
-// The sign convention of givensAlgorithm: flip (c, s, r) when |f| > |g| and c < 0.
-__device__ __forceinline__ bool givens_flip(double f, double g, double c)
-{
-    const uint64_t af = abs_bits(f), ag = abs_bits(g);
-    return af > ag && !nan_bits(af) && !nan_bits(ag) && is_negative(c);
-}
-
-// LinearAlgebra.givensAlgorithm (LAPACK 3.2 DLARTG port), as called by get_rotation.
-__device__ __forceinline__ void givens(double f, double g, double& cs, double& sn, double& r)
-{
-    const double safmn2 = 0x1p-485;
-    const double safmx2 = 0x1p+485;
-    if (g == 0.0) {
-        cs = 1.0; sn = 0.0; r = f;
-    } else if (f == 0.0) {
-        cs = 0.0; sn = 1.0; r = g;
-    } else {
-        double f1 = f, g1 = g;
-        double scale = jl_max(fabs(f1), fabs(g1));
-        if (scale >= safmx2) {
-            int count = 0;
-            do {
-                ++count;
-                f1 = __dmul_rn(f1, safmn2); g1 = __dmul_rn(g1, safmn2);
-                scale = jl_max(fabs(f1), fabs(g1));
-            } while (scale >= safmx2 && count < 20);
-            r = __dsqrt_rn(__dadd_rn(__dmul_rn(f1, f1), __dmul_rn(g1, g1)));
-            cs = __ddiv_rn(f1, r); sn = __ddiv_rn(g1, r);
-            for (int i = 0; i < count; ++i) r = __dmul_rn(r, safmx2);
-        } else if (scale <= safmn2) {
-            int count = 0;
-            do {
-                ++count;
-                f1 = __dmul_rn(f1, safmx2); g1 = __dmul_rn(g1, safmx2);
-                scale = jl_max(fabs(f1), fabs(g1));
-            } while (scale <= safmn2 && count < 64);  // 64 steps cover every subnormal
-            r = __dsqrt_rn(__dadd_rn(__dmul_rn(f1, f1), __dmul_rn(g1, g1)));
-            cs = __ddiv_rn(f1, r); sn = __ddiv_rn(g1, r);
-            for (int i = 0; i < count; ++i) r = __dmul_rn(r, safmn2);
-        } else {
-            r = __dsqrt_rn(__dadd_rn(__dmul_rn(f1, f1), __dmul_rn(g1, g1)));
-            cs = __ddiv_rn(f1, r); sn = __ddiv_rn(g1, r);
-        }
-        if (fabs(f) > fabs(g) && cs < 0.0) { cs = -cs; sn = -sn; r = -r; }
-    }
-}
-
-// givensAlgorithm with its branch tests on the integer pipe and its products issued as FMAs
-// (same results as givens()); the rare branches fall back to givens().
-__device__ __forceinline__ void givens_fast(double f, double g, double& cs, double& sn, double& r,
-                                            double nz)
-{
-    if (givens_case(f, g) != 4) {
-        givens(f, g, cs, sn, r);
-        return;
-    }
-    r = __dsqrt_rn(__dadd_rn(mulz(f, f, nz), mulz(g, g, nz)));
-    cs = __ddiv_rn(f, r);
-    sn = __ddiv_rn(g, r);
-    if (givens_flip(f, g, cs)) { cs = neg(cs); sn = neg(sn); r = neg(r); }
-}
+using namespace gv;
 
 // is_offdiagonal_small(H, j, tol), 1-based j (src/bulge_chasing.jl:7-8).
 __device__ __forceinline__ bool is_small(const double* dv, const double* ev, int64_t j, double tol)
@@ -175,6 +78,8 @@ __device__ __forceinline__ void record(double* grid, int32_t* thick, int32_t* pl
 // single_shift!(H, from, to, mu, givens, layer_thickness) (src/bulge_chasing.jl:11-144).
 // dv/ev are 0-based arrays; from/to 1-based.  Values the sweep itself produced travel in
 // registers; only untouched entries are loaded.
+// NR = true computes each rotation by givens_nr (proved Newton form, else the reference form).
+template <bool NR>
 __device__ void single_shift(double* __restrict__ dv, double* __restrict__ ev, int64_t from,
                              int64_t to, double mu, double* __restrict__ grid,
                              int32_t* __restrict__ thick, int32_t* __restrict__ place,
@@ -182,7 +87,8 @@ __device__ void single_shift(double* __restrict__ dv, double* __restrict__ ev, i
 {
     const double H11 = dv[from - 1], H21 = ev[from - 1], H22 = dv[from];
     double c, s, nrm;
-    givens_fast(__dsub_rn(H11, mu), H21, c, s, nrm, nz);
+    if (NR) givens_nr(__dsub_rn(H11, mu), H21, mulz(H21, H21, nz), c, s, nrm, nz);
+    else givens_fast(__dsub_rn(H11, mu), H21, c, s, nrm, nz);
     const double H11p = fsum(c, H11, s, H21, nz);
     const double H21p = fdif(c, H21, s, H11, nz);
     const double H12p = fsum(c, H21, s, H22, nz);
@@ -213,7 +119,8 @@ __device__ void single_shift(double* __restrict__ dv, double* __restrict__ ev, i
         // prefetch for step i+1: dv[i+2], ev[i+2] (1-based)
         if (i + 1 <= to - 1) B22_n = dv[i + 1];
         if (i + 3 <= to) B23_n = ev[i + 1];
-        givens_fast(p1, bulge, c, s, nrm, nz);
+        if (NR) givens_nr(p1, bulge, mulz(bulge, bulge, nz), c, s, nrm, nz);
+        else givens_fast(p1, bulge, c, s, nrm, nz);
         ev[i - 2] = nrm;
         const double B21 = e_next;
         const double B11p = fsum(c, B11, s, B21, nz);
@@ -237,27 +144,33 @@ __device__ void single_shift(double* __restrict__ dv, double* __restrict__ ev, i
     }
 }
 
-// ---- the sweep on two warps ------------------------------------------------------------------
+// ---- the sweep on two warps, Newton-form rotations -------------------------------------
 //
 // single_shift! is one dependency chain per step: (f, g) -> r = sqrt(f^2 + g^2) -> c = f/r,
-// s = g/r -> the 2x2 update -> next (f, g).  On GB300 each FP64 instruction holds its SM
-// sub-partition's FP64 unit ~64 cycles, so the step time is the number of FP64 instructions
-// the chain's warp issues.  Two warps on two sub-partitions split a step:
-//   warp 0 (the chain): f*f, sqrt, c = f/r, s*B21, s*B22, B11', B12', B11'*s, B12'' -> next f;
-//   warp 1: s = g/r, next bulge (= next g) and its square, next B21, the B21'/B22'/B22''
-//           updates (-> next B11), B11'', every store and the rotation record.
-// They trade values through a two-slot shared mailbox (slot = step parity) and five named
-// barriers, each used producer -> consumer (bar.arrive / bar.sync) except the (c, s)
-// exchange.  Every value and every rounding is the one the one-thread sweep computes.
-enum : int { kBarR = 1, kBarCS = 2, kBarG = 3, kBarB = 4, kBarP = 5 };
+// s = g/r -> the 2x2 update -> next (f, g).  On GB300 one warp issues an FP64 instruction
+// about every 64-90 cycles whatever their dependences, and the SM runs a few such warps at
+// once, so the step time is set by the FP64 instructions on the warp that carries the chain.
+// Here (the fastest split measured)
+//   warp 0 (the chain): the rotation by givens_nr_core (14 FP64 instructions), the four
+//           products of the 2x2 update that give the next f (B11', B12', B11'*s, B12'') and
+//           the next bulge g = s*ev[i+1] with g*g;
+//   warp 1: next B21 = c*ev[i+1] and the B21'/B22'/B22'' half of the update (-> next B11),
+//           B11'', the rounding proof of warp 0's rotation, every store and the record.
+// They trade values through a two-slot shared mailbox (slot = step parity) and two named
+// barriers, each used producer -> consumer (bar.arrive / bar.sync) and each strictly
+// alternating: warp 0 waits for B(i-1) before it arrives at CS(i), and warp 1 arrives at
+// B(i) only after CS(i).
+// Warp 0 does not wait for the proof.  Warp 1 records a failed proof (none was seen in 10^9
+// random rotations; see givens.cuh) and the kernel then restores the sweep's entries from a
+// copy taken before it and runs the sweep again in the reference form (single_shift), so the
+// result is bit-identical either way.  Steps whose (f, g) are outside the Newton form's range
+// take givens_fast on warp 0 and skip the proof.
+enum : int { kBarCS = 1, kBarB = 2 };
 
-struct Mail {
-    double r, f;            // warp 0 -> 1 (kBarR)
-    double c, s;            // exchanged (kBarCS)
-    double bulge, e_next, gg;  // warp 1 -> 0 (kBarG): next g, next B21, next g*g
-    double b22pp;           // warp 1 -> 0 (kBarB): next B11
-    double b11p, b12p, b12pp;  // warp 0 -> 1 (kBarP)
-    int mode;               // 0: warp 1 divides; 1: warp 0 ran the full givensAlgorithm
+struct NrMail {
+    double c, s, r, x, f, g;  // warp 0 -> 1 (kBarCS); r with the sign convention applied
+    int32_t slow;             // 1: (c, s, r) from givens_fast, nothing to prove
+    double b22pp, e_next;     // warp 1 -> 0 (kBarB): next B11, next B21
 };
 
 __device__ __forceinline__ void nb_sync(int id)
@@ -271,116 +184,98 @@ __device__ __forceinline__ void nb_arrive(int id)
 
 // single_shift!(H, from, to, mu, givens, layer_thickness) (src/bulge_chasing.jl:11-144) by
 // both warps of the CTA.  Step i (1-based, from .. to-1) is the reference's first rotation
-// for i = from and its loop body otherwise; both have the same 2x2 update.
-__device__ void single_shift_2w(double* __restrict__ dv, double* __restrict__ ev, int64_t from,
-                                int64_t to, double mu, double* __restrict__ grid,
-                                int32_t* __restrict__ thick, int32_t* __restrict__ place,
-                                int64_t rows, int32_t layer, double nz, Mail* mail)
+// for i = from and its loop body otherwise; both have the same 2x2 update.  Of the entries the
+// reference writes and later overwrites within the sweep only the final ones are stored:
+// dv[from-1 .. to-1] (0-based), ev[from-1 .. to-3] = the norms r of steps from+1 .. to-1 and
+// ev[to-2] = the last B12''.  The grid slot of rotation i is column `layer` (exact order) or
+// thick[i-1] + 1 (the reference's placement; thick is updated by the caller after the sweep).
+// *fail is set when a Newton-form rotation could not be proved.
+__device__ void sweep_nr_2w(double* __restrict__ dv, double* __restrict__ ev, int64_t from,
+                            int64_t to, double mu, double* __restrict__ grid,
+                            const int32_t* __restrict__ thick, int64_t rows, int32_t layer,
+                            double nz, NrMail* mail, int32_t* fail)
 {
     const int warp = threadIdx.x >> 5;
     const bool lead = (threadIdx.x & 31) == 0;
     const double H11 = dv[from - 1], H21 = ev[from - 1];
-    double B11 = H11, B21 = H21;
-    double B22n = dv[from];                                  // dv[i+1] (1-based) for step i
-    double B23n = (from + 2 <= to) ? ev[from] : 0.0;         // ev[i+1] (1-based) for step i
     if (warp == 0) {
         double f = __dsub_rn(H11, mu), g = H21, gg = mulz(H21, H21, nz);
+        double B11 = H11, B21 = H21;
+        double B22n = dv[from];                                  // dv[i+1] (1-based) for step i
+        double B23n = (from + 2 <= to) ? ev[from] : 0.0;         // ev[i+1] (1-based) for step i
         for (int64_t i = from; i <= to - 1; ++i) {
-            Mail& mb = mail[i & 1];
-            const double B22 = B22n;
-            if (i + 1 <= to - 1) B22n = dv[i + 1];
-            if (i > from) {
-                nb_sync(kBarG);
-                const Mail& pv = mail[(i - 1) & 1];
-                g = pv.bulge;
-                B21 = pv.e_next;
-                gg = pv.gg;
-            }
-            double c, s, r;
-            const int mode = givens_case(f, g) == 4 ? 0 : 1;
-            if (mode == 0) {
-                r = __dsqrt_rn(__dadd_rn(mulz(f, f, nz), gg));
-                mb.r = r; mb.f = f; mb.mode = 0;
-                nb_arrive(kBarR);
-                c = __ddiv_rn(f, r);
-                mb.c = c;
-            } else {
-                givens(f, g, c, s, r);
-                mb.r = r; mb.f = f; mb.mode = 1; mb.c = c; mb.s = s;
-                nb_arrive(kBarR);
-            }
-            nb_sync(kBarCS);
-            if (mode == 0) {
-                s = mb.s;
-                if (givens_flip(f, g, c)) { c = neg(c); s = neg(s); }
-            }
-            if (i > from) {
-                nb_sync(kBarB);
-                B11 = mail[(i - 1) & 1].b22pp;
-            }
-            const double sB21 = mulz(s, B21, nz), sB22 = mulz(s, B22, nz);
-            const double B11p = __fma_rn(c, B11, sB21);
-            const double B12p = __fma_rn(c, B21, sB22);
-            const double B12pp = __fma_rn(B12p, c, neg(mulz(B11p, s, nz)));
-            mb.b11p = B11p; mb.b12p = B12p; mb.b12pp = B12pp;
-            nb_arrive(kBarP);
-            f = B12pp;
-        }
-    } else {
-        double g = H21;
-        for (int64_t i = from; i <= to - 1; ++i) {
-            Mail& mb = mail[i & 1];
             const double B22 = B22n, B23 = B23n;
             if (i + 1 <= to - 1) B22n = dv[i + 1];
             if (i + 3 <= to) B23n = ev[i + 1];
-            nb_sync(kBarR);
-            double r = mb.r;
-            const double f = mb.f;
-            const int mode = mb.mode;
-            double s = 0.0;
-            if (mode == 0) {
-                s = __ddiv_rn(g, r);
-                mb.s = s;
+            // the Newton form whatever the range (no branch before the chain), then the
+            // reference form when the inputs are out of its range
+            const NrRot o = givens_nr_core(f, g, gg, nz);
+            double c = o.c, s = o.s, r = o.r;
+            int32_t slow = 0;
+            if (!nr_in_range(f, g)) {
+                givens_fast(f, g, c, s, r, nz);
+                slow = 1;
             }
+            if (i > from) {
+                nb_sync(kBarB);
+                const NrMail& pv = mail[(i - 1) & 1];
+                B11 = pv.b22pp;
+                B21 = pv.e_next;
+            }
+            NrMail& mb = mail[i & 1];
+            mb.c = c; mb.s = s; mb.r = r; mb.x = o.x; mb.f = f; mb.g = g; mb.slow = slow;
+            nb_arrive(kBarCS);
+            const double B11p = __fma_rn(c, B11, mulz(s, B21, nz));
+            const double B12p = __fma_rn(c, B21, mulz(s, B22, nz));
+            f = __fma_rn(B12p, c, -mulz(B11p, s, nz));
+            g = (i + 2 <= to) ? mulz(s, B23, nz) : 0.0;
+            gg = mulz(g, g, nz);
+        }
+    } else {
+        double B11 = H11, B21 = H21;
+        double B22n = dv[from];
+        double B23n = (from + 2 <= to) ? ev[from] : 0.0;
+        int32_t thn = layer <= 0 ? thick[from - 1] : 0;
+        bool bad = false;
+        for (int64_t i = from; i <= to - 1; ++i) {
+            const double B22 = B22n, B23 = B23n;
+            const int32_t th = thn;
+            if (i + 1 <= to - 1) B22n = dv[i + 1];
+            if (i + 3 <= to) B23n = ev[i + 1];
+            if (layer <= 0 && i + 1 <= to - 1) thn = thick[i];
             nb_sync(kBarCS);
-            double c = mb.c;
-            if (mode == 0) {
-                if (givens_flip(f, g, c)) { c = neg(c); s = neg(s); r = neg(r); }
-            } else {
-                s = mb.s;
-            }
-            double bulge = 0.0, e_next = 0.0;
-            if (i + 2 <= to) {
-                bulge = mulz(s, B23, nz);
-                e_next = mulz(c, B23, nz);
-            }
-            if (i < to - 1) {
-                mb.bulge = bulge; mb.e_next = e_next; mb.gg = mulz(bulge, bulge, nz);
-                nb_arrive(kBarG);
-            }
-            const double sB11 = mulz(s, B11, nz), sB21 = mulz(s, B21, nz);
-            const double B21p = __fma_rn(c, B21, neg(sB11));
-            const double B22p = __fma_rn(c, B22, neg(sB21));
-            const double B22pp = __fma_rn(B22p, c, neg(mulz(B21p, s, nz)));
+            NrMail& mb = mail[i & 1];
+            const double c = mb.c, s = mb.s, r = mb.r, x = mb.x, f = mb.f, g = mb.g;
+            const int32_t slow = mb.slow;
+            const double e_next = (i + 2 <= to) ? mulz(c, B23, nz) : 0.0;
+            const double sB21 = mulz(s, B21, nz);
+            const double B21p = __fma_rn(c, B21, -mulz(s, B11, nz));
+            const double B22p = __fma_rn(c, B22, -sB21);
+            const double B22pp = __fma_rn(B22p, c, -mulz(B21p, s, nz));
             if (i < to - 1) {
                 mb.b22pp = B22pp;
+                mb.e_next = e_next;
                 nb_arrive(kBarB);
             }
-            nb_sync(kBarP);
-            const double B11p = mb.b11p, B12p = mb.b12p, B12pp = mb.b12pp;
+            const double B11p = __fma_rn(c, B11, sB21);
+            const double B12p = __fma_rn(c, B21, mulz(s, B22, nz));
             const double B11pp = __fma_rn(B11p, c, mulz(B12p, s, nz));
+            if (!slow && !givens_nr_proved(f, g, x, c, s, r)) bad = true;
             if (lead) {
-                if (i > from) ev[i - 2] = r;
                 dv[i - 1] = B11pp;
-                dv[i] = B22pp;
-                ev[i - 1] = B12pp;
-                if (i + 2 <= to) ev[i] = e_next;
-                record(grid, thick, place, rows, i, layer, c, s);
+                if (i > from) ev[i - 2] = r;
+                const int32_t L = layer > 0 ? layer : th + 1;
+                *reinterpret_cast<double2*>(grid + 2 * ((i - 1) + (int64_t)(L - 1) * rows)) =
+                    make_double2(c, s);
+                if (i == to - 1) {
+                    dv[i] = B22pp;
+                    ev[i - 1] = __fma_rn(B12p, c, -mulz(B11p, s, nz));
+                }
             }
-            g = bulge;
             B11 = B22pp;
             B21 = e_next;
         }
+        if (lead && bad) *fail = 1;
     }
 }
 
@@ -394,7 +289,7 @@ __device__ __forceinline__ int32_t warp_max(int32_t v)
 // One flush: the reference's inner loop from `to = last_block_ends_at` until the matrix is
 // split into converged parts, every block has reached max_layers, or iter > maxiter.
 // Warp 0 runs the control flow and the O(n) scans with ballots; each sweep runs on both
-// warps (single_shift_2w).
+// warps (sweep_nr_2w) after both copy the entries it may change to `bak` (2n doubles).
 //
 // Exact-order placement (st->exact_order != 0).  The reference applies a flush's grid in
 // layer-major order, which equals the order the chase made the rotations only while every
@@ -414,10 +309,12 @@ struct Decision {
 
 __global__ void __launch_bounds__(64, 1)
 chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __restrict__ ev,
-             double* __restrict__ grid, int32_t* __restrict__ thick, int32_t* __restrict__ place)
+             double* __restrict__ grid, int32_t* __restrict__ thick, int32_t* __restrict__ place,
+             double* __restrict__ bak)
 {
-    __shared__ Mail mail[2];
+    __shared__ NrMail mail[2];
     __shared__ Decision dec;
+    __shared__ int32_t fail;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int64_t n = st->n;
@@ -428,14 +325,17 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
     const int32_t grid_layers = st->grid_layers;
     const bool exact = st->exact_order != 0;
     const int64_t maxiter = st->maxiter;
+    const int32_t mode = st->chase_mode;
     int64_t iter = st->iter;
     int64_t lbe = st->last_block_ends_at;
     const int64_t rows = n > 1 ? n - 1 : 1;
+    int64_t redone = 0;
 
     for (int64_t q = threadIdx.x; q < n; q += 64) {
         thick[q] = 0;
         place[q] = 0;
     }
+    if (threadIdx.x == 0) fail = 0;
     __syncthreads();
 
     bool did = false;
@@ -514,8 +414,41 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
         }
         __syncthreads();
         const Decision d = dec;
-        if (d.action == 1)
-            single_shift_2w(dv, ev, d.from, d.to, d.mu, grid, thick, place, rows, d.layer, nz, mail);
+        if (d.action == 1) {
+            // entries the sweep may change: dv[from-1 .. to-1], ev[from-1 .. to-2] (0-based)
+            const int64_t q0 = d.from - 1, q1 = d.to - 1;
+            bool redo = mode == 1;
+            if (mode != 1) {
+                for (int64_t q = q0 + threadIdx.x; q <= q1; q += 64) {
+                    bak[q] = dv[q];
+                    if (q < q1) bak[n + q] = ev[q];
+                }
+                __syncthreads();
+                sweep_nr_2w(dv, ev, d.from, d.to, d.mu, grid, thick, rows, d.layer, nz, mail, &fail);
+                __syncthreads();
+                redo = fail != 0 || mode == 2;
+                if (redo) {
+                    for (int64_t q = q0 + threadIdx.x; q <= q1; q += 64) {
+                        dv[q] = bak[q];
+                        if (q < q1) ev[q] = bak[n + q];
+                    }
+                    ++redone;
+                }
+            }
+            if (redo) {
+                // the reference form on one thread; it updates thick/place itself
+                __syncthreads();
+                if (threadIdx.x == 0)
+                    single_shift<false>(dv, ev, d.from, d.to, d.mu, grid, thick, place, rows, d.layer, nz);
+                if (threadIdx.x == 0) fail = 0;
+            } else {
+                for (int64_t q = q0 + threadIdx.x; q < q1; q += 64) {
+                    const int32_t t = thick[q] + 1;
+                    thick[q] = t;
+                    place[q] = d.layer > 0 ? d.layer : t;
+                }
+            }
+        }
         __syncthreads();
         if (d.action == 0) break;  // both warps leave on the same decision
     }
@@ -535,6 +468,7 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
             st->max_thickness = kmax;
             st->total_rotations += rotations;
             st->early_flushes += early;
+            st->redone_sweeps += redone;
         }
     }
 }
@@ -602,7 +536,7 @@ __device__ void chase_flush_lane(ChaseState* __restrict__ st, double* __restrict
                         }
                 }
                 const double mu = wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
-                single_shift(dv, ev, from, to, mu, grid, thick, place, rows, layer, st->neg_zero);
+                single_shift<true>(dv, ev, from, to, mu, grid, thick, place, rows, layer, st->neg_zero);
                 did = true;
                 iter += 1;
                 rotations += to - from;
@@ -645,9 +579,9 @@ chase_batched_kernel(const BatchMat* __restrict__ mats, const int32_t* __restric
 }  // namespace
 
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
-                         int32_t* place, cudaStream_t stream)
+                         int32_t* place, double* bak, cudaStream_t stream)
 {
-    chase_kernel<<<1, 64, 0, stream>>>(state, d, e, grid, thick, place);
+    chase_kernel<<<1, 64, 0, stream>>>(state, d, e, grid, thick, place, bak);
     return cudaGetLastError();
 }
 

@@ -72,7 +72,11 @@ struct ChaseState {
     int64_t max_thickness;       // thickest column of the rotation grid (placement layers)
     int64_t total_rotations;
     int64_t early_flushes;       // flushes ended because a sweep's layer exceeded grid_layers
-    double  neg_zero;            // -0.0, supplied at run time (see mulz in chase.cu)
+    double  neg_zero;            // -0.0, supplied at run time (see mulz in givens.cuh)
+    int32_t chase_mode;          // 0 Newton-form two-warp sweeps, 1 reference form on one
+                                 // thread, 2 Newton form with every sweep redone (tests)
+    int32_t pad0;
+    int64_t redone_sweeps;       // sweeps run again in the reference form (cumulative)
 };
 
 // ---- launch helpers (defined in the .cu files) ------------------------------------------
@@ -108,7 +112,7 @@ void apply_set_shape(int fp64, int shape);
 int apply_get_shape(int fp64);
 
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
-                         int32_t* place, cudaStream_t stream);
+                         int32_t* place, double* bak, cudaStream_t stream);
 
 // One matrix of a batch: size and offsets into the packed arrays (elements, not bytes).
 struct BatchMat {

@@ -147,3 +147,36 @@ def test_qr_reference_placement_and_exact_order(cuda, pkg, oracle, n, seed):
     Qx = out[True][1]
     assert np.array_equal(Qx, tQ)
     assert np.linalg.norm(T @ Qx - Qx * out[True][0]) / np.linalg.norm(T) <= 10 * n * eps
+
+
+def _wide(n, seed):
+    """Entries spanning 2^-600 .. 2^600 with tiny couplings: many chase steps fall outside the
+    Newton form's range and take the reference-form rotation."""
+    rng = np.random.default_rng(seed)
+    d = rng.standard_normal(n) * 2.0 ** rng.integers(-600, 600, n)
+    e = rng.random(n - 1) * 2.0 ** rng.integers(-600, 600, n - 1)
+    return d, e
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2])
+@pytest.mark.parametrize("kind,n", [("A", 64), ("B", 129), ("C", 200), ("split", 96),
+                                    ("graded", 50), ("wide", 80)])
+def test_qr_chase_modes_bit_exact(cuda, pkg, oracle, mode, kind, n):
+    """Every chase mode (Newton-form two-warp sweeps, reference form, Newton form with every
+    sweep restored and redone) gives the oracle's bits; mode 2 also counts its redone sweeps."""
+    d, e = _wide(n, seed=n) if kind == "wide" else tridiag(kind, n, seed=n)
+    od, oe, oQ = d.copy(), e.copy(), np.asfortranarray(np.eye(n))
+    conv_o, it_o, _, _ = oracle.qr_algorithm(od, oe, oQ)
+    H = pkg.SymTridiagonal(d.copy(), e.copy())
+    Q = np.asfortranarray(np.eye(n))
+    h = pkg.Handle(0)
+    _, conv, it = pkg.qr_algorithm_(H, Q, handle=h, chase_mode=mode)
+    assert (conv, it) == (conv_o, it_o)
+    assert np.array_equal(H.dv, od)
+    assert np.array_equal(H.ev, oe)
+    assert np.array_equal(Q, oQ)
+    st = h.stats()
+    if mode == 2:
+        assert st["redone_sweeps"] == it
+    else:
+        assert st["redone_sweeps"] == 0
