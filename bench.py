@@ -48,7 +48,7 @@ def parse_args():
     p.add_argument("--n", type=int, default=16384)
     p.add_argument("--k", type=int, default=64)
     p.add_argument("--no-extras", action="store_true", help="skip the FP32 and n=2000 side measurements")
-    p.add_argument("--workload", choices=["apply", "solve"], default="apply",
+    p.add_argument("--workload", choices=["apply", "solve", "batched", "adjoint"], default="apply",
                    help="apply: the bulk-apply microbenchmark (default); solve: one full qr_algorithm!")
     p.add_argument("--case", choices=["A", "B"], default="A",
                    help="solve workload: A d_i = i, e ~ U[0,1) (seed 1); B d ~ N(0,1), e ~ 0.5 N(0,1) (seed 2)")
@@ -57,6 +57,9 @@ def parse_args():
                    help="solve workload: also run the CPU oracle's chase (eigenvalues only) and compare bits")
     p.add_argument("--chase-mode", type=int, choices=[0, 1, 2], default=0,
                    help="solve workload: 0 Newton-form two-warp chase, 1 reference form, 2 Newton + redo")
+    p.add_argument("--count", type=int, default=4096, help="batched workload: number of tridiagonals")
+    p.add_argument("--loop-sample", type=int, default=16,
+                   help="batched workload: matrices timed one launch per matrix (extrapolated by sum n^2)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     return p.parse_args()
 
@@ -457,12 +460,226 @@ def run_solve(args):
     h.close()
 
 
+def _tq_errors(torch, d, e, lam, Q):
+    """||TQ - Q diag(lam)||_F / ||T||_F and ||Q^T Q - I||_F in FP64 on the GPU."""
+    TQ = d[:, None] * Q
+    TQ[:-1] += e[:, None] * Q[1:]
+    TQ[1:] += e[:, None] * Q[:-1]
+    normT = math.sqrt(float((d * d).sum() + 2 * (e * e).sum()))
+    resid = float(torch.linalg.norm(TQ - Q * lam[None, :])) / normT
+    G = Q.T @ Q
+    G.diagonal().sub_(1.0)
+    return resid, float(torch.linalg.norm(G))
+
+
+def run_batched(args):
+    """Batched eigensolves (qr_algorithm_batched_, symeig_qr_batched_f64_dev): `count`
+    tridiagonals with n ~ U{32..1024}, d ~ N(0,1), e ~ U[0.1,1) (seed 3), FP64 Q, solved by
+    the persistent work-queue path with CUDA-graph rounds and the autotuned tile shapes, versus
+    one qr_algorithm! call per matrix on the same GPU, timed on a sample of the matrices and
+    extrapolated by sum n^2 (the loop over all 4096 would take about an hour).  Errors: every
+    matrix's eigenvalues against LAPACK, residual and orthogonality of a sample."""
+    import torch
+    import __graft_entry__ as ge
+    from scipy.linalg import eigh_tridiagonal
+    pkg = ge.load_package()
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    h = pkg.Handle(0)
+    tuning = pkg.batched_autotune(handle=h)
+    rng = np.random.default_rng(3)
+    count = args.count
+    sizes = rng.integers(32, 1025, size=count)
+    d = rng.standard_normal(int(sizes.sum()))
+    e = rng.random(int((sizes - 1).sum())) * 0.9 + 0.1
+    td, te = torch.from_numpy(d.copy()).to(dev), torch.from_numpy(e.copy()).to(dev)
+    tQ = torch.zeros(int((sizes * sizes).sum()), dtype=torch.float64, device=dev)
+    off = 0
+    for n in sizes:
+        tQ[off:off + n * n].view(n, n).fill_diagonal_(1.0)
+        off += n * n
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        conv, iters = pkg.qr_algorithm_batched_(td, te, sizes, tQ, handle=h)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+    st = h.stats()
+    lam_all = td.cpu().numpy()
+    # errors: every matrix's eigenvalues vs LAPACK; residual / orthogonality on a sample
+    eig_ratio, resid_max, orth_max = 0.0, 0.0, 0.0
+    eps = float(np.finfo(np.float64).eps)
+    od = oe = oq = 0
+    check = set(rng.choice(count, min(64, count), replace=False).tolist())
+    for k, n in enumerate(sizes):
+        n = int(n)
+        dk, ek = d[od:od + n], e[oe:oe + n - 1]
+        ref = eigh_tridiagonal(dk, ek, eigvals_only=True)
+        err = float(np.max(np.abs(np.sort(lam_all[od:od + n]) - ref)))
+        eig_ratio = max(eig_ratio, err / (10 * n * eps * float(np.max(np.abs(ref)))))
+        if k in check:
+            Qk = tQ[oq:oq + n * n].view(n, n).T
+            r, o = _tq_errors(torch, torch.from_numpy(dk).to(dev), torch.from_numpy(ek).to(dev), td[od:od + n], Qk)
+            resid_max, orth_max = max(resid_max, r / (10 * n * eps)), max(orth_max, o / (10 * n * eps))
+        od += n; oe += n - 1; oq += n * n
+    # one launch per matrix on a sample
+    sample = rng.choice(count, min(args.loop_sample, count), replace=False)
+    loop_s, work = 0.0, 0.0
+    for k in sample:
+        n = int(sizes[k])
+        dd = torch.from_numpy(rng.standard_normal(n)).to(dev)
+        ee = torch.from_numpy(rng.random(n - 1) * 0.9 + 0.1).to(dev)
+        Q = torch.eye(n, dtype=torch.float64, device=dev).T
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pkg.qr_algorithm_(pkg.SymTridiagonal(dd, ee), Q, handle=h)
+        torch.cuda.synchronize()
+        loop_s += time.perf_counter() - t0
+        work += n * n
+    loop_est = loop_s * float((sizes.astype(np.float64) ** 2).sum()) / work
+    out = {
+        "metric": f"batched eigensolves per second, {count} tridiagonals n~U{{32..1024}}",
+        "value": round(count / secs, 2), "unit": "solves/s", "higher_is_better": True, "n_gpus": 1,
+        "dtype": "f64", "data": "synthetic (seed 3: n ~ U{32..1024}, d ~ N(0,1), e ~ U[0.1,1))",
+        "config": {"workload": "qr_algorithm_batched_ (persistent work queue, CUDA-graph rounds)",
+                   "count": count, "max_layers": 128},
+        "seconds": round(secs, 3), "all_converged": bool(conv.all()), "iterations": int(iters.sum()),
+        "rounds": st["flushes"], "tuning": tuning[0],
+        "loop": {"solves_per_s": round(count / loop_est, 3), "sample": int(len(sample)),
+                 "sample_seconds": round(loop_s, 2), "extrapolated_seconds": round(loop_est, 1)},
+        "speedup_vs_loop": round(loop_est / secs, 1),
+        "errors": {"eig_err_over_10n_eps_normT_max": eig_ratio, "resid_over_10n_eps_max": resid_max,
+                   "orth_over_10n_eps_max": orth_max, "sampled_matrices": len(check)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out), flush=True)
+    h.close()
+
+
+def run_adjoint(args):
+    """Adjoint of the eigensolve (TridiagEigh: forward qr_algorithm!, backward
+    symeig_eig_adjoint_f64_dev): n = 4096, d ~ N(0,1), e ~ U[0.1,1) (seed 4), loss
+    L = sum_i w_i lam_(i) + sum_{i<=64} q_(i)^T B q_(i), w ~ N(0,1), B symmetric ~ N(0,1/n),
+    eigenpairs sorted ascending.  Reports (forward + backward) / forward time and the gradient
+    against an FP64 reference (LAPACK eigenpairs and the closed-form pullback in numpy); the
+    finite-difference check runs in the tests at smaller n.  Then the batched variant
+    (TridiagEighBatched) on 256 matrices of n = 512."""
+    import torch
+    import __graft_entry__ as ge
+    from scipy.linalg import eigh_tridiagonal
+    pkg = ge.load_package()
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    n, K = (args.n if args.n != 16384 else 4096), 64
+    rng = np.random.default_rng(4)
+    d = rng.standard_normal(n)
+    e = rng.random(n - 1) * 0.9 + 0.1
+    w = rng.standard_normal(n)
+    Bm = rng.standard_normal((n, n)) / np.sqrt(n)
+    Bm = (Bm + Bm.T) / 2
+    tw, tB = torch.tensor(w, device=dev), torch.tensor(Bm, device=dev)
+
+    def loss(lam, Q):
+        order = torch.argsort(lam)
+        QK = Q[:, order][:, :K]
+        return (tw * lam[order]).sum() + (QK * (tB @ QK)).sum()
+
+    # one untimed pass of the whole path at n = 256 (library and kernel loading)
+    wd = torch.tensor(d[:256], device=dev, requires_grad=True)
+    we = torch.tensor(e[:255], device=dev, requires_grad=True)
+    wl, wQ = pkg.TridiagEigh.apply(wd, we)
+    wo = torch.argsort(wl)
+    wK = wQ[:, wo][:, :K]
+    ((tw[:256] * wl[wo]).sum() + (wK * (tB[:256, :256] @ wK)).sum()).backward()
+    torch.cuda.synchronize()
+    td = torch.tensor(d, device=dev, requires_grad=True)
+    te = torch.tensor(e, device=dev, requires_grad=True)
+    with ClockSampler(0) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lam, Q = pkg.TridiagEigh.apply(td, te)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        L = loss(lam, Q)
+        torch.cuda.synchronize()
+        tl = time.perf_counter()
+        L.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+    fwd, loss_s, bwd = t1 - t0, tl - t1, t2 - tl
+    # FP64 reference gradient
+    lam_r, V = eigh_tridiagonal(d, e)
+    gV = np.zeros((n, n))
+    gV[:, :K] = 2 * Bm @ V[:, :K]
+    F = lam_r[None, :] - lam_r[:, None]
+    np.fill_diagonal(F, 1.0)
+    F = 1.0 / F
+    np.fill_diagonal(F, 0.0)
+    A = V @ (np.diag(w) + F * (V.T @ gV)) @ V.T
+    g_ref = np.concatenate([np.diag(A), np.diag(A, 1) + np.diag(A, -1)])
+    g = np.concatenate([td.grad.cpu().numpy(), te.grad.cpu().numpy()])
+    rel = float(np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref))
+    # the adjoint kernels alone (two FP64 tensor-core GEMMs with fused epilogues)
+    glam = torch.randn(n, device=dev, dtype=torch.float64)
+    gQ = torch.randn(n, n, device=dev, dtype=torch.float64)
+    lam_d, Q_d = lam.detach(), Q.detach()
+    pkg.eig_adjoint(lam_d, Q_d, glam, gQ)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    pkg.eig_adjoint(lam_d, Q_d, glam, gQ)
+    e1.record()
+    torch.cuda.synchronize()
+    adj_ms = e0.elapsed_time(e1)
+    # batched variant: 256 matrices of n = 512
+    B, nb = 256, 512
+    db = torch.tensor(rng.standard_normal((B, nb)), device=dev, requires_grad=True)
+    eb = torch.tensor(rng.random((B, nb - 1)) * 0.9 + 0.1, device=dev, requires_grad=True)
+    wb = torch.tensor(rng.standard_normal((B, nb)), device=dev)
+    Bb = torch.tensor(rng.standard_normal((nb, nb)) / np.sqrt(nb), device=dev)
+    Bb = (Bb + Bb.T) / 2
+    # untimed pass of the batched path on 4 matrices
+    w4d, w4e = db[:4].detach().clone().requires_grad_(True), eb[:4].detach().clone().requires_grad_(True)
+    l4, Q4 = pkg.TridiagEighBatched.apply(w4d, w4e)
+    o4 = torch.argsort(l4, dim=1)
+    K4 = torch.gather(Q4, 2, o4[:, None, :8].expand(4, nb, 8))
+    ((wb[:4] * torch.gather(l4, 1, o4)).sum() + (K4 * (Bb @ K4)).sum()).backward()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lamb, Qb = pkg.TridiagEighBatched.apply(db, eb)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ob = torch.argsort(lamb, dim=1)
+    QKb = torch.gather(Qb, 2, ob[:, None, :8].expand(B, nb, 8))
+    Lb = (wb * torch.gather(lamb, 1, ob)).sum() + (QKb * (Bb @ QKb)).sum()
+    Lb.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    out = {
+        "metric": f"adjoint (forward + backward) / forward time, n={n}",
+        "value": round((fwd + loss_s + bwd) / fwd, 4), "unit": "ratio", "higher_is_better": False, "n_gpus": 1,
+        "dtype": "f64", "data": "synthetic (seed 4: d ~ N(0,1), e ~ U[0.1,1), w ~ N(0,1), B ~ N(0,1/n) symmetric)",
+        "config": {"workload": "TridiagEigh forward + backward, loss on the 64 lowest eigenpairs", "n": n, "K": K},
+        "forward_s": round(fwd, 3), "loss_s": round(loss_s, 3), "backward_s": round(bwd, 3),
+        "grad_rel_err_vs_fp64_reference": rel,
+        "adjoint_kernels_ms": round(adj_ms, 2),
+        "adjoint_gemm_tflops": round(4.0 * n ** 3 / (adj_ms * 1e-3) / 1e12, 3),
+        "batched": {"B": B, "n": nb, "forward_s": round(t1 - t0, 3), "backward_s": round(t2 - t1, 3),
+                    "ratio": round((t2 - t0) / (t1 - t0), 4)},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "solve":
         run_solve(args)
+    elif args.workload == "batched":
+        run_batched(args)
+    elif args.workload == "adjoint":
+        run_adjoint(args)
     else:
         run_ours(args)
 

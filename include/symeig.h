@@ -217,6 +217,14 @@ int symeig_apply_givens_left_f64_dev(symeig_handle h, double* A, int64_t lda, in
 int symeig_apply_givens_left_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t m,
                                      int64_t n, const float* cs, int64_t k);
 
+/* get_rotation(f, g) -> (c, s, r) (src/simple_givens.jl:20-23, LinearAlgebra.givensAlgorithm)
+ * elementwise on `count` pairs, computed on the device the way the chase computes them (the
+ * proved Newton form, or the reference form when symeig_set_chase_mode(h, 1)); both give the
+ * reference's bits.  Host arrays (copied) or, for _dev, device arrays on the handle's stream. */
+int symeig_get_rotation_f64(symeig_handle h, int64_t count, const double* f, const double* g,
+                            double* c, double* s, double* r);
+int symeig_get_rotation_f64_dev(symeig_handle h, int64_t count, const double* f, const double* g,
+                                double* c, double* s, double* r);
 /* ---- eigen_decomp!  (src/bulge_chasing.jl:290-299) ----------------------------------- *
  * Q (n x n, ldq >= n) is set to the identity, then qr_algorithm! runs with the default
  * max_layers = 128, tol = eps, maxiter = 100n.  d/e overwritten as in symeig_qr_f64. */

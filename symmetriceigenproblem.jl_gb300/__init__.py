@@ -14,6 +14,7 @@ from .api import (  # noqa: F401
     batched_autotune,
     qr_algorithm_batched_,
     eigen_decomp_,
+    get_rotation,
     givens_buffer,
     qr_algorithm_,
 )

@@ -88,6 +88,38 @@ def _colmajor_info(A):
     return A.ctypes.data, max(ld, m, 1), m, n, dt, False
 
 
+def get_rotation(f, g, handle: Handle | None = None, form: int = 0):
+    """get_rotation(f, g) -> (c, s, r) elementwise (src/simple_givens.jl:20-23,
+    LinearAlgebra.givensAlgorithm), computed on the device the way the chase computes them:
+    form 0 the proved Newton form, form 1 the reference form.  f, g: float64 numpy arrays
+    (host) or CUDA tensors (device) of one shape."""
+    dev = _is_torch(f)
+    h = handle or default_handle(f.device.index if dev else 0)
+    h.set_chase_mode(1 if form == 1 else 0)
+    try:
+        if dev:
+            if f.dtype != torch.float64 or g.dtype != torch.float64 or f.shape != g.shape:
+                raise TypeError("f, g must be float64 CUDA tensors of one shape")
+            fc, gc = f.contiguous().reshape(-1), g.contiguous().reshape(-1)
+            c, s, r = (torch.empty_like(fc) for _ in range(3))
+            with h.on_stream(torch.cuda.current_stream(f.device).cuda_stream):
+                h.call("symeig_get_rotation_f64_dev", int(fc.numel()), ctypes.c_void_p(fc.data_ptr()),
+                       ctypes.c_void_p(gc.data_ptr()), ctypes.c_void_p(c.data_ptr()),
+                       ctypes.c_void_p(s.data_ptr()), ctypes.c_void_p(r.data_ptr()))
+            return c.reshape(f.shape), s.reshape(f.shape), r.reshape(f.shape)
+        fa = np.ascontiguousarray(f, dtype=np.float64).reshape(-1)
+        ga = np.ascontiguousarray(g, dtype=np.float64).reshape(-1)
+        if fa.shape != ga.shape:
+            raise ValueError("f and g must have one shape")
+        c, s, r = (np.empty_like(fa) for _ in range(3))
+        h.call("symeig_get_rotation_f64", int(fa.size), fa.ctypes.data, ga.ctypes.data, c.ctypes.data,
+               s.ctypes.data, r.ctypes.data)
+        shp = np.shape(f)
+        return c.reshape(shp), s.reshape(shp), r.reshape(shp)
+    finally:
+        h.set_chase_mode(0)
+
+
 def givens_buffer(n_minus_1: int, k: int, dtype=np.float64) -> np.ndarray:
     """An uninitialised Julia-layout Matrix{Tuple{T,T}} of shape (n-1, k, 2)."""
     return np.empty((k, n_minus_1, 2), dtype=dtype).transpose(1, 0, 2)

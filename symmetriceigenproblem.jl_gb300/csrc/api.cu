@@ -54,7 +54,7 @@ struct symeig_context {
     cudaEvent_t ev_chased[2] = {nullptr, nullptr};
     cudaEvent_t ev_consumed[2] = {nullptr, nullptr};
     cudaEvent_t ev_main = nullptr;
-    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs, bak;
+    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs, bak, rot;
     int* derr = nullptr;   // device error word of the wave kernels (bounded waits)
     int32_t exact_order = 1;  // rotation placement of the qr driver
     int32_t chase_mode = 0;   // symeig_set_chase_mode
@@ -492,7 +492,7 @@ int symeig_destroy(symeig_handle h)
         if (h->ev_consumed[b]) cudaEventDestroy(h->ev_consumed[b]);
     }
     h->table.release(); h->state.release(); h->d.release(); h->e.release();
-    h->q.release(); h->cs.release(); h->bak.release();
+    h->q.release(); h->cs.release(); h->bak.release(); h->rot.release();
     if (h->ev_main) cudaEventDestroy(h->ev_main);
     for (cudaEvent_t ev : h->timing) cudaEventDestroy(ev);
     for (cudaEvent_t ev : h->kpool) cudaEventDestroy(ev);
@@ -784,6 +784,43 @@ int symeig_eig_adjoint_f64(symeig_handle h, int64_t count, int64_t n, const doub
     CK(cudaMemcpyAsync(gd, dgd, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (ne) CK(cudaMemcpyAsync(ge, dge, ne * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    return SYMEIG_OK;
+}
+
+int symeig_get_rotation_f64_dev(symeig_handle h, int64_t count, const double* f, const double* g,
+                                double* c, double* s, double* r)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (count < 0) return SYMEIG_ERR_SIZE;
+    if (count > 0 && (!f || !g || !c || !s || !r)) return SYMEIG_ERR_NULL;
+    begin_call(h);
+    CK(launch_get_rotation(count, f, g, c, s, r, h->chase_mode == 1 ? 1 : 0, h->stream));
+    return SYMEIG_OK;
+}
+
+int symeig_get_rotation_f64(symeig_handle h, int64_t count, const double* f, const double* g,
+                            double* c, double* s, double* r)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (count < 0 || count > ((int64_t)1 << 40)) return SYMEIG_ERR_SIZE;
+    if (count == 0) return SYMEIG_OK;
+    if (!f || !g || !c || !s || !r) return SYMEIG_ERR_NULL;
+    const size_t b = (size_t)count * sizeof(double);
+    CK(h->rot.ensure(5 * b));
+    double* base = (double*)h->rot.ptr;
+    double *df = base, *dg = base + count, *dc = base + 2 * count, *ds = base + 3 * count,
+           *dr = base + 4 * count;
+    cudaStream_t st = h->stream;
+    CK(cudaMemcpyAsync(df, f, b, cudaMemcpyHostToDevice, st));
+    CK(cudaMemcpyAsync(dg, g, b, cudaMemcpyHostToDevice, st));
+    rc = symeig_get_rotation_f64_dev(h, count, df, dg, dc, ds, dr);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(c, dc, b, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(s, ds, b, cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(r, dr, b, cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
     return SYMEIG_OK;
 }
 

@@ -576,7 +576,35 @@ chase_batched_kernel(const BatchMat* __restrict__ mats, const int32_t* __restric
     chase_flush_lane(st, d + mt.doff, e + mt.eoff, grids + mt.goff, thick + mt.doff, place + mt.doff);
 }
 
+// get_rotation(f, g) (src/simple_givens.jl:20-23) elementwise: form 0 the chase's Newton form
+// (givens_nr), form 1 the reference form (givens).
+__global__ void get_rotation_kernel(int64_t count, const double* __restrict__ f,
+                                    const double* __restrict__ g, double* __restrict__ c,
+                                    double* __restrict__ s, double* __restrict__ r, int32_t form,
+                                    double nz)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < count;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        const double fi = f[i], gi = g[i];
+        double ci, si, ri;
+        if (form == 1) givens(fi, gi, ci, si, ri);
+        else givens_nr(fi, gi, mulz(gi, gi, nz), ci, si, ri, nz);
+        c[i] = ci;
+        s[i] = si;
+        r[i] = ri;
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_get_rotation(int64_t count, const double* f, const double* g, double* c,
+                                double* s, double* r, int32_t form, cudaStream_t stream)
+{
+    if (count <= 0) return cudaSuccess;
+    const int64_t blocks = (count + 255) / 256 < 1216 ? (count + 255) / 256 : 1216;
+    get_rotation_kernel<<<(unsigned)blocks, 256, 0, stream>>>(count, f, g, c, s, r, form, -0.0);
+    return cudaGetLastError();
+}
 
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
                          int32_t* place, double* bak, cudaStream_t stream)

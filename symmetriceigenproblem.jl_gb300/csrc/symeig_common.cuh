@@ -111,6 +111,9 @@ cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t g
 void apply_set_shape(int fp64, int shape);
 int apply_get_shape(int fp64);
 
+// givensAlgorithm elementwise on device arrays (form 0 Newton form, 1 reference form).
+cudaError_t launch_get_rotation(int64_t count, const double* f, const double* g, double* c,
+                                double* s, double* r, int32_t form, cudaStream_t stream);
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
                          int32_t* place, double* bak, cudaStream_t stream);
 

@@ -64,3 +64,41 @@ def test_device_qr_matches_golden(cuda, pkg, idx):
     assert (conv, it) == (cse["conv"], cse["iter"])
     assert np.array_equal(H.dv, unhex(cse["d_out"]))
     assert np.array_equal(Q.ravel(order="F"), unhex(cse["Q_out_colmajor"]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("form", [0, 1])
+def test_device_get_rotation_matches_golden(cuda, pkg, form):
+    """The device's rotation generator (form 0: the chase's proved Newton form; form 1: the
+    reference form) reproduces the independent restatement's (c, s, r) bits."""
+    cases = json.loads((GOLDEN / "golden_givens.json").read_text())
+    f = np.array([float.fromhex(c["f"]) for c in cases])
+    g = np.array([float.fromhex(c["g"]) for c in cases])
+    c, s, r = pkg.get_rotation(f, g, form=form)
+    want = np.array([[float.fromhex(x) for x in cse["csr"]] for cse in cases])
+    got = np.stack([c, s, r], axis=1)
+    assert np.array_equal(got.view(np.uint64), want.view(np.uint64))
+
+
+@pytest.mark.gpu
+def test_device_get_rotation_random_matches_oracle(cuda, pkg, oracle):
+    """2^20 random pairs with chase-like and wide exponents: Newton form == reference form ==
+    the C oracle's givensAlgorithm, bit for bit (signed zeros included)."""
+    rng = np.random.default_rng(77)
+    m = 1 << 20
+    e1 = np.where(rng.random(m) < 0.8, rng.integers(-30, 31, m), rng.integers(-1000, 1001, m))
+    e2 = np.where(rng.random(m) < 0.8, e1 + rng.integers(-30, 31, m), rng.integers(-1000, 1001, m))
+    f = rng.standard_normal(m) * np.ldexp(1.0, e1)
+    g = rng.standard_normal(m) * np.ldexp(1.0, np.clip(e2, -1070, 1000))
+    f[::97] = 0.0
+    g[::89] = 0.0
+    import torch
+    tf, tg = torch.from_numpy(f).cuda(), torch.from_numpy(g).cuda()
+    c0, s0, r0 = (t.cpu().numpy() for t in pkg.get_rotation(tf, tg, form=0))
+    c1, s1, r1 = pkg.get_rotation(f, g, form=1)
+    sample = rng.choice(m, 4096, replace=False)
+    oc = np.array([oracle.givens(float(f[i]), float(g[i])) for i in sample])
+    for a, b in ((c0, c1), (s0, s1), (r0, r1)):
+        assert np.array_equal(a.view(np.uint64), b.view(np.uint64))
+    got = np.stack([c0[sample], s0[sample], r0[sample]], axis=1)
+    assert np.array_equal(got.view(np.uint64), oc.view(np.uint64))
