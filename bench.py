@@ -48,7 +48,7 @@ def parse_args():
     p.add_argument("--n", type=int, default=16384)
     p.add_argument("--k", type=int, default=64)
     p.add_argument("--no-extras", action="store_true", help="skip the FP32 and n=2000 side measurements")
-    p.add_argument("--workload", choices=["apply", "solve", "batched", "adjoint"], default="apply",
+    p.add_argument("--workload", choices=["apply", "solve", "batched", "adjoint", "dense"], default="apply",
                    help="apply: the bulk-apply microbenchmark (default); solve: one full qr_algorithm!")
     p.add_argument("--case", choices=["A", "B"], default="A",
                    help="solve workload: A d_i = i, e ~ U[0,1) (seed 1); B d ~ N(0,1), e ~ 0.5 N(0,1) (seed 2)")
@@ -670,6 +670,75 @@ def run_adjoint(args):
     print(json.dumps(out), flush=True)
 
 
+def run_dense(args):
+    """Dense symmetric eigensolve on the device (syev: sytrd -> orgtr -> qr_algorithm!), the
+    step before the reference's path: A symmetric with N(0,1) entries (seed 5), n = --n
+    (default 4096).  Reports each phase's time, the reduction's throughput ((4/3) n^3 flops
+    for sytrd and as many for orgtr) and the errors; the CPU baseline is LAPACK dsytrd + dorgtr
+    (scipy, all host cores) on the same matrix."""
+    import torch
+    import __graft_entry__ as ge
+    from scipy.linalg import lapack
+    pkg = ge.load_package()
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    n = args.n if args.n != 16384 else 4096
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((n, n))
+    A = np.asfortranarray((A + A.T) / 2)
+    h = pkg.Handle(0)
+    # warm-up at a small order
+    w = np.asfortranarray(A[:96, :96])
+    pkg.syev(torch.from_numpy(w.T.copy()).to(dev).T, handle=h)
+    tA = torch.from_numpy(A.T.copy()).to(dev).T
+    torch.cuda.synchronize()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        d, e, tau = pkg.sytrd_(tA, handle=h)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        V = pkg.orgtr(tA, tau, handle=h)
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        _, conv, it = pkg.qr_algorithm_(pkg.SymTridiagonal(d, e), V, handle=h)
+        torch.cuda.synchronize()
+        t3 = time.perf_counter()
+    lam = d
+    tA0 = torch.from_numpy(A.T.copy()).to(dev).T
+    resid = float(torch.linalg.norm(tA0 @ V - V * lam[None, :]) / torch.linalg.norm(tA0))
+    G = V.T @ V
+    G.diagonal().sub_(1.0)
+    orth = float(torch.linalg.norm(G))
+    ref = np.linalg.eigvalsh(A)
+    eig_err = float(np.max(np.abs(np.sort(lam.cpu().numpy()) - ref)))
+    eps = float(np.finfo(np.float64).eps)
+    flops = 4.0 / 3.0 * n ** 3
+    out = {
+        "metric": f"dense symmetric eigensolve seconds, n={n}",
+        "value": round(t3 - t0, 3), "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f64",
+        "data": "synthetic (seed 5: symmetric, N(0,1) entries)",
+        "config": {"workload": "syev: sytrd -> orgtr -> qr_algorithm!", "n": n},
+        "sytrd_s": round(t1 - t0, 3), "orgtr_s": round(t2 - t1, 3), "qr_s": round(t3 - t2, 3),
+        "sytrd_gflops": round(flops / (t1 - t0) / 1e9, 1), "orgtr_gflops": round(flops / (t2 - t1) / 1e9, 1),
+        "converged": bool(conv), "iterations": it,
+        "errors": {"eig_max_abs_vs_lapack": eig_err, "eig_bound_10n_eps_normA": 10 * n * eps * float(np.max(np.abs(ref))),
+                   "resid_rel": resid, "orth": orth, "bound_10n_eps": 10 * n * eps},
+        "clocks": clk.summary(),
+    }
+    if not args.no_cpu_baseline:
+        t0 = time.perf_counter()
+        c, dl, el, taul, info = lapack.dsytrd(A, lower=1)
+        t1 = time.perf_counter()
+        ql, _, info2 = lapack.dorgqr(np.asfortranarray(c[1:, : n - 1]), taul)   # dorgtr (lower)
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"value": round(t2 - t0, 3), "unit": "s (sytrd + orgtr)", "cores": os.cpu_count(),
+                               "kind": "LAPACK (scipy dsytrd + dorgtr)", "sytrd_s": round(t1 - t0, 3),
+                               "orgtr_s": round(t2 - t1, 3),
+                               "sample": f"the same n={n} matrix, scipy's LAPACK on all host cores"}
+    print(json.dumps(out), flush=True)
+    h.close()
+
+
 def main():
     args = parse_args()
     if args.impl == "reference":
@@ -680,6 +749,8 @@ def main():
         run_batched(args)
     elif args.workload == "adjoint":
         run_adjoint(args)
+    elif args.workload == "dense":
+        run_dense(args)
     else:
         run_ours(args)
 

@@ -217,6 +217,27 @@ int symeig_apply_givens_left_f64_dev(symeig_handle h, double* A, int64_t lda, in
 int symeig_apply_givens_left_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t m,
                                      int64_t n, const float* cs, int64_t k);
 
+/* Dense symmetric -> tridiagonal, the step before qr_algorithm! (no reference counterpart:
+ * the reference's callers supply a SymTridiagonal).  LAPACK dsytrd / dorgtr semantics, lower:
+ * A (n x n, both triangles stored, column-major, lda) = Q T Q^T, T = SymTridiagonal(d, e);
+ * on exit A's diagonal and subdiagonal hold T and the Householder vectors lie below, tau
+ * (n-1) holds their scalars.  orgtr forms Q (n x n, ldq) from them.  syev is the dense
+ * eigensolve: sytrd, orgtr into V, then qr_algorithm!(SymTridiagonal(lam, e), V): lam the
+ * (unsorted) eigenvalues, V the eigenvectors; the device version overwrites A, the host
+ * version leaves it unchanged.  Results match LAPACK within rounding (not bit for bit). */
+int symeig_sytrd_f64(symeig_handle h, int64_t n, double* A, int64_t lda, double* d, double* e,
+                     double* tau);
+int symeig_sytrd_f64_dev(symeig_handle h, int64_t n, double* A, int64_t lda, double* d, double* e,
+                         double* tau);
+int symeig_orgtr_f64(symeig_handle h, int64_t n, const double* A, int64_t lda, const double* tau,
+                     double* Q, int64_t ldq);
+int symeig_orgtr_f64_dev(symeig_handle h, int64_t n, const double* A, int64_t lda, const double* tau,
+                         double* Q, int64_t ldq);
+int symeig_syev_f64(symeig_handle h, int64_t n, const double* A, int64_t lda, double* lam, double* V,
+                    int64_t ldv, int32_t* converged, int64_t* iter);
+int symeig_syev_f64_dev(symeig_handle h, int64_t n, double* A, int64_t lda, double* lam, double* V,
+                        int64_t ldv, int32_t* converged, int64_t* iter);
+
 /* get_rotation(f, g) -> (c, s, r) (src/simple_givens.jl:20-23, LinearAlgebra.givensAlgorithm)
  * elementwise on `count` pairs, computed on the device the way the chase computes them (the
  * proved Newton form, or the reference form when symeig_set_chase_mode(h, 1)); both give the

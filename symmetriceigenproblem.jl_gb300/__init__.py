@@ -16,7 +16,10 @@ from .api import (  # noqa: F401
     eigen_decomp_,
     get_rotation,
     givens_buffer,
+    orgtr,
     qr_algorithm_,
+    syev,
+    sytrd_,
 )
 from ._lib import Handle, SymeigError, default_handle, load as load_library  # noqa: F401
 from .build import build, LIB as LIBRARY_PATH  # noqa: F401

@@ -34,6 +34,12 @@ SIGNATURES = {
     "symeig_set_exact_order": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_chase_mode": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_get_rotation_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "symeig_sytrd_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "symeig_sytrd_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp]),
+    "symeig_orgtr_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_i64]),
+    "symeig_orgtr_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_i64]),
+    "symeig_syev_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp]),
+    "symeig_syev_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp]),
     "symeig_get_rotation_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "symeig_set_kernel_timing": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, c_i32, ctypes.POINTER(c_dbl)]),

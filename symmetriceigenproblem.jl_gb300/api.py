@@ -299,6 +299,76 @@ def batched_autotune(handle: Handle | None = None):
     return {"split": split.value, "shape_small": s0.value, "shape_large": s1.value}, [list(ms[0:2]), list(ms[2:4])]
 
 
+def _dense_square(A, what="A"):
+    ptr, ld, m, n, dt, dev = _colmajor_info(A)
+    if m != n:
+        raise ValueError(f"{what} must be square")
+    if dt != "f64":
+        raise TypeError(f"{what} must be float64")
+    return ptr, ld, n, dev
+
+
+def sytrd_(A, handle: Handle | None = None):
+    """Dense symmetric -> tridiagonal (LAPACK dsytrd, lower; no reference counterpart: the
+    step before qr_algorithm! for a dense symmetric A).  A (n x n, both triangles, column-major,
+    float64; numpy or CUDA torch) is overwritten as by dsytrd.  Returns (d, e, tau) with
+    A = Q SymTridiagonal(d, e) Q^T, Q = orgtr(A, tau)."""
+    ptr, ld, n, dev = _dense_square(A)
+    h = handle or default_handle(A.device.index if dev else 0)
+    if dev:
+        d = torch.empty(n, dtype=torch.float64, device=A.device)
+        e = torch.empty(max(n - 1, 0), dtype=torch.float64, device=A.device)
+        tau = torch.empty(max(n - 1, 0), dtype=torch.float64, device=A.device)
+        with h.on_stream(torch.cuda.current_stream(A.device).cuda_stream):
+            h.call("symeig_sytrd_f64_dev", n, ctypes.c_void_p(ptr), ld, ctypes.c_void_p(d.data_ptr()),
+                   ctypes.c_void_p(e.data_ptr() if n > 1 else None), ctypes.c_void_p(tau.data_ptr() if n > 1 else None))
+        return d, e, tau
+    d, e, tau = np.empty(n), np.empty(max(n - 1, 0)), np.empty(max(n - 1, 0))
+    h.call("symeig_sytrd_f64", n, ctypes.c_void_p(ptr), ld, d.ctypes.data,
+           ctypes.c_void_p(e.ctypes.data if n > 1 else None), ctypes.c_void_p(tau.ctypes.data if n > 1 else None))
+    return d, e, tau
+
+
+def orgtr(A, tau, handle: Handle | None = None):
+    """Q of sytrd_ (LAPACK dorgtr, lower) as a new column-major matrix."""
+    ptr, ld, n, dev = _dense_square(A)
+    h = handle or default_handle(A.device.index if dev else 0)
+    if dev:
+        Q = torch.empty(n, n, dtype=torch.float64, device=A.device).T
+        t = tau.contiguous()
+        with h.on_stream(torch.cuda.current_stream(A.device).cuda_stream):
+            h.call("symeig_orgtr_f64_dev", n, ctypes.c_void_p(ptr), ld,
+                   ctypes.c_void_p(t.data_ptr() if n > 1 else None), ctypes.c_void_p(Q.data_ptr()), n)
+        return Q
+    Q = np.empty((n, n), order="F")
+    t = np.ascontiguousarray(tau, dtype=np.float64)
+    h.call("symeig_orgtr_f64", n, ctypes.c_void_p(ptr), ld, ctypes.c_void_p(t.ctypes.data if n > 1 else None),
+           Q.ctypes.data, n)
+    return Q
+
+
+def syev(A, handle: Handle | None = None):
+    """Dense symmetric eigensolve on the device: sytrd, orgtr, then qr_algorithm! on the
+    tridiagonal with Q = the orthogonal factor.  Returns (lam, V, converged, iters): lam
+    unsorted as the reference's H.dv, V the eigenvectors (column-major).  A CUDA tensor A is
+    overwritten (as by sytrd_); a numpy A is left unchanged."""
+    ptr, ld, n, dev = _dense_square(A)
+    h = handle or default_handle(A.device.index if dev else 0)
+    conv, it = c_i32(), c_i64()
+    if dev:
+        lam = torch.empty(n, dtype=torch.float64, device=A.device)
+        V = torch.empty(n, n, dtype=torch.float64, device=A.device).T
+        with h.on_stream(torch.cuda.current_stream(A.device).cuda_stream):
+            h.call("symeig_syev_f64_dev", n, ctypes.c_void_p(ptr), ld, ctypes.c_void_p(lam.data_ptr()),
+                   ctypes.c_void_p(V.data_ptr()), n, ctypes.byref(conv), ctypes.byref(it))
+        return lam, V, bool(conv.value), int(it.value)
+    lam = np.empty(n)
+    V = np.empty((n, n), order="F")
+    h.call("symeig_syev_f64", n, ctypes.c_void_p(ptr), ld, lam.ctypes.data, V.ctypes.data, n,
+           ctypes.byref(conv), ctypes.byref(it))
+    return lam, V, bool(conv.value), int(it.value)
+
+
 def eig_adjoint(lam, Q, glam, gQ=None, handle: Handle | None = None):
     """dL/d(d, e) of the tridiagonal eigensolve from dL/dlam and dL/dQ (symeig_eig_adjoint_f64*).
 

@@ -18,7 +18,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libsymeig.so"
-SOURCES = ["apply.cu", "chase.cu", "api.cu", "peak.cu", "noalloc.cu", "batched.cu", "adjoint.cu"]
+SOURCES = ["apply.cu", "chase.cu", "api.cu", "peak.cu", "noalloc.cu", "batched.cu", "adjoint.cu", "sytrd.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "-Xcompiler", "-Wall", "-Xcompiler", "-Wextra", "-Xcompiler", "-Wno-unused-parameter",

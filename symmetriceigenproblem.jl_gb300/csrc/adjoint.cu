@@ -10,8 +10,8 @@
 // autograd Function of the host bindings.  Q is the solver's output, so no rotation history
 // is stored.
 //
-// Two FP64 tensor-core GEMMs (mma.sync m8n8k4 .f64, the FP64 MMA of sm_103a; tcgen05 has no
-// f64 kind) with fused epilogues:
+// Two FP64 tensor-core GEMMs (dmma_tile.cuh: mma.sync m8n8k4 .f64, the FP64 MMA of sm_103a;
+// tcgen05 has no f64 kind) with fused epilogues:
 //   1. G = Q^T gQ, epilogue M_ij = i == j ? glam_i : G_ij / (lam_j - lam_i), M stored.
 //   2. P = Q M, epilogue: per row i the partial sums over the CTA's columns k of
 //        P_ik Q_ik (-> dd_i),  P_ik Q_{i+1,k} and P_ik Q_{i-1,k} (-> de_i, de_{i-1}),
@@ -22,72 +22,14 @@
 
 #include "symeig.h"
 #include "symeig_common.cuh"
+#include "dmma_tile.cuh"
 
 namespace symeig {
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 16;  // CTA tile
-constexpr int kAdjThreads = 128;           // 4 warps, 2 x 2, each 32 x 32
-constexpr int SPAD = 2;                    // smem row padding (doubles)
-
-__device__ __forceinline__ void dmma(double (&c)[2], double a, double b)
-{
-    asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0, %1}, {%2}, {%3}, {%0, %1};"
-                 : "+d"(c[0]), "+d"(c[1]) : "d"(a), "d"(b));
-}
-
-// C[BM x BN] tile of op(A)[M x K] * B[K x N] for one CTA.  A is addressed as A(i, k) at
-// a + i * a_si + k * a_sk, B(k, j) at b + k + j * ldb (k contiguous).  Out-of-range elements
-// read as 0.  acc[mi][nj][2]: the warp's 4 x 4 grid of 8 x 8 MMA tiles.
-struct TileGemm {
-    __device__ static void run(const double* __restrict__ a, int64_t a_si, int64_t a_sk,
-                               const double* __restrict__ b, int64_t ldb, int64_t M, int64_t N,
-                               int64_t K, int64_t i0, int64_t j0, double (&acc)[4][4][2],
-                               double (*As)[BK + SPAD], double (*Bs)[BK + SPAD])
-    {
-        const int tid = threadIdx.x;
-        const int warp = tid >> 5, lane = tid & 31;
-        const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
-        const int grp = lane >> 2, tig = lane & 3;
-#pragma unroll
-        for (int x = 0; x < 4; ++x)
-#pragma unroll
-            for (int y = 0; y < 4; ++y) acc[x][y][0] = acc[x][y][1] = 0.0;
-        const bool a_kcontig = (a_sk == 1);
-        for (int64_t k0 = 0; k0 < K; k0 += BK) {
-            // stage A (BM x BK) and B (BN x BK, k contiguous) tiles; 8 elements per thread each
-#pragma unroll
-            for (int q = 0; q < (BM * BK) / kAdjThreads; ++q) {
-                const int e = tid + q * kAdjThreads;
-                int r, kk;
-                if (a_kcontig) { r = e / BK; kk = e % BK; } else { kk = e / BM; r = e % BM; }
-                const int64_t gi = i0 + r, gk = k0 + kk;
-                As[r][kk] = (gi < M && gk < K) ? a[gi * a_si + gk * a_sk] : 0.0;
-            }
-#pragma unroll
-            for (int q = 0; q < (BN * BK) / kAdjThreads; ++q) {
-                const int e = tid + q * kAdjThreads;
-                const int c = e / BK, kk = e % BK;
-                const int64_t gj = j0 + c, gk = k0 + kk;
-                Bs[c][kk] = (gj < N && gk < K) ? b[gk + gj * ldb] : 0.0;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int ks = 0; ks < BK; ks += 4) {
-                double af[4], bf[4];
-#pragma unroll
-                for (int x = 0; x < 4; ++x) af[x] = As[wm + x * 8 + grp][ks + tig];
-#pragma unroll
-                for (int y = 0; y < 4; ++y) bf[y] = Bs[wn + y * 8 + grp][ks + tig];
-#pragma unroll
-                for (int x = 0; x < 4; ++x)
-#pragma unroll
-                    for (int y = 0; y < 4; ++y) dmma(acc[x][y], af[x], bf[y]);
-            }
-            __syncthreads();
-        }
-    }
-};
+using dmma::BM;
+using dmma::BN;
+constexpr int kAdjThreads = dmma::kThreads;
 
 // 1. M = diag(glam) + F o (Q^T gQ), M column-major with leading dimension n.
 __global__ void __launch_bounds__(kAdjThreads)
@@ -96,8 +38,7 @@ adjoint_m_kernel(const double* __restrict__ Q, int64_t ldq, const double* __rest
                  int64_t n, double* __restrict__ Mout, int64_t strideQ, int64_t strideG,
                  int64_t strideM)
 {
-    __shared__ double As[BM][BK + SPAD];
-    __shared__ double Bs[BN][BK + SPAD];
+    __shared__ dmma::Smem sm;
     const int64_t z = blockIdx.z;
     Q += z * strideQ;
     gQ += z * strideG;
@@ -106,8 +47,8 @@ adjoint_m_kernel(const double* __restrict__ Q, int64_t ldq, const double* __rest
     glam += z * n;
     const int64_t i0 = (int64_t)blockIdx.y * BM, j0 = (int64_t)blockIdx.x * BN;
     double acc[4][4][2];
-    // A(i, k) = Q(k, i): k contiguous
-    TileGemm::run(Q, ldq, 1, gQ, ldg, n, n, n, i0, j0, acc, As, Bs);
+    // A(i, k) = Q(k, i): k contiguous; B(k, j) = gQ(k, j): k contiguous
+    dmma::tile_gemm(Q, ldq, 1, gQ, 1, ldg, n, n, n, i0, j0, 0, n, acc, sm);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
     const int grp = lane >> 2, tig = lane & 3;
@@ -138,8 +79,7 @@ adjoint_p_kernel(const double* __restrict__ Q, int64_t ldq, const double* __rest
                  int64_t n, double* __restrict__ part, int64_t strideQ, int64_t strideM,
                  int64_t stridePart)
 {
-    __shared__ double As[BM][BK + SPAD];
-    __shared__ double Bs[BN][BK + SPAD];
+    __shared__ dmma::Smem sm;
     __shared__ double red[3][2][BM];
     const int64_t z = blockIdx.z;
     Q += z * strideQ;
@@ -148,7 +88,7 @@ adjoint_p_kernel(const double* __restrict__ Q, int64_t ldq, const double* __rest
     const int64_t i0 = (int64_t)blockIdx.y * BM, k0 = (int64_t)blockIdx.x * BN;
     double acc[4][4][2];
     // A(i, j) = Q(i, j): i contiguous; B(j, k) = M(j, k): j contiguous
-    TileGemm::run(Q, 1, ldq, M, n, n, n, n, i0, k0, acc, As, Bs);
+    dmma::tile_gemm(Q, 1, ldq, M, 1, n, n, n, n, i0, k0, 0, n, acc, sm);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
     const int grp = lane >> 2, tig = lane & 3;

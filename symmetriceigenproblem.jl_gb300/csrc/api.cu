@@ -13,6 +13,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -54,7 +55,7 @@ struct symeig_context {
     cudaEvent_t ev_chased[2] = {nullptr, nullptr};
     cudaEvent_t ev_consumed[2] = {nullptr, nullptr};
     cudaEvent_t ev_main = nullptr;
-    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs, bak, rot;
+    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs, bak, rot, dense, dense_io;
     int* derr = nullptr;   // device error word of the wave kernels (bounded waits)
     int32_t exact_order = 1;  // rotation placement of the qr driver
     int32_t chase_mode = 0;   // symeig_set_chase_mode
@@ -417,6 +418,41 @@ int apply_left_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, co
 
 }  // namespace
 
+namespace {
+
+// sytrd with an exact power-of-two prescaling of A (see sytrd.cu on the range of the norms).
+// work: dense_scratch_doubles(n) + 1 doubles on the device.
+int sytrd_scaled(symeig_handle h, int64_t n, double* A, int64_t lda, double* d, double* e, double* tau,
+                 double* work)
+{
+    cudaStream_t st = h->stream;
+    double* amax_d = work + dense_scratch_doubles(n);
+    CK(launch_dense_maxabs(A, lda, n, amax_d, st));
+    double amax = 0.0;
+    CK(cudaMemcpyAsync(&amax, amax_d, sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    int ea = 0;
+    const bool scale = amax != 0.0 && std::isfinite(amax) && ((ea = std::ilogb(amax)) < -2 || ea > 2);
+    if (scale) CK(launch_dense_scale(A, lda, n, std::ldexp(1.0, -ea), st));
+    int rc = sytrd_dev(st, n, A, lda, d, e, tau, work);
+    if (rc) return rc;
+    if (scale) CK(launch_tridiag_unscale(A, lda, n, d, e, std::ldexp(1.0, ea), st));
+    return SYMEIG_OK;
+}
+
+int dense_args(symeig_handle h, int64_t n, const void* A, int64_t lda)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n < 1 || n > ((int64_t)1 << 30)) return SYMEIG_ERR_SIZE;
+    if (!A) return SYMEIG_ERR_NULL;
+    if (lda < n) return SYMEIG_ERR_LD;
+    if (mul_overflows(lda, n)) return SYMEIG_ERR_SIZE;
+    return SYMEIG_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int symeig_apply_givens_left_f64(symeig_handle h, double* A, int64_t lda, int64_t m, int64_t n,
@@ -493,6 +529,7 @@ int symeig_destroy(symeig_handle h)
     }
     h->table.release(); h->state.release(); h->d.release(); h->e.release();
     h->q.release(); h->cs.release(); h->bak.release(); h->rot.release();
+    h->dense.release(); h->dense_io.release();
     if (h->ev_main) cudaEventDestroy(h->ev_main);
     for (cudaEvent_t ev : h->timing) cudaEventDestroy(ev);
     for (cudaEvent_t ev : h->kpool) cudaEventDestroy(ev);
@@ -784,6 +821,125 @@ int symeig_eig_adjoint_f64(symeig_handle h, int64_t count, int64_t n, const doub
     CK(cudaMemcpyAsync(gd, dgd, nv * sizeof(double), cudaMemcpyDeviceToHost, s));
     if (ne) CK(cudaMemcpyAsync(ge, dge, ne * sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    return SYMEIG_OK;
+}
+
+int symeig_sytrd_f64_dev(symeig_handle h, int64_t n, double* A, int64_t lda, double* d, double* e,
+                         double* tau)
+{
+    int rc = dense_args(h, n, A, lda);
+    if (rc) return rc;
+    if (!d || (n > 1 && (!e || !tau))) return SYMEIG_ERR_NULL;
+    begin_call(h);
+    CK(h->dense.ensure((size_t)(dense_scratch_doubles(n) + 1) * sizeof(double)));
+    return sytrd_scaled(h, n, A, lda, d, e, tau, (double*)h->dense.ptr);
+}
+
+int symeig_orgtr_f64_dev(symeig_handle h, int64_t n, const double* A, int64_t lda, const double* tau,
+                         double* Q, int64_t ldq)
+{
+    int rc = dense_args(h, n, A, lda);
+    if (rc) return rc;
+    if (!Q || (n > 1 && !tau)) return SYMEIG_ERR_NULL;
+    if (ldq < n) return SYMEIG_ERR_LD;
+    begin_call(h);
+    CK(h->dense.ensure((size_t)(dense_scratch_doubles(n) + 1) * sizeof(double)));
+    return orgtr_dev(h->stream, n, A, lda, tau, Q, ldq, (double*)h->dense.ptr);
+}
+
+int symeig_syev_f64_dev(symeig_handle h, int64_t n, double* A, int64_t lda, double* lam, double* V,
+                        int64_t ldv, int32_t* converged, int64_t* iter)
+{
+    int rc = dense_args(h, n, A, lda);
+    if (rc) return rc;
+    if (!lam || !V || !converged || !iter) return SYMEIG_ERR_NULL;
+    if (ldv < n) return SYMEIG_ERR_LD;
+    begin_call(h);
+    const size_t ws = (size_t)dense_scratch_doubles(n) + 1;
+    CK(h->dense.ensure((ws + 2 * (size_t)n) * sizeof(double)));
+    double* work = (double*)h->dense.ptr;
+    double* e = work + ws;
+    double* tau = e + n;
+    rc = sytrd_scaled(h, n, A, lda, lam, e, tau, work);
+    if (rc) return rc;
+    rc = orgtr_dev(h->stream, n, A, lda, tau, V, ldv, work);
+    if (rc) return rc;
+    const double eps = 2.220446049250313e-16;
+    return qr_dev<double>(h, lam, e, n, V, ldv, n, 128, eps, 100 * n, converged, iter);
+}
+
+int symeig_sytrd_f64(symeig_handle h, int64_t n, double* A, int64_t lda, double* d, double* e,
+                     double* tau)
+{
+    int rc = dense_args(h, n, A, lda);
+    if (rc) return rc;
+    if (!d || (n > 1 && (!e || !tau))) return SYMEIG_ERR_NULL;
+    const size_t nn = (size_t)n * n;
+    CK(h->dense_io.ensure((nn + 3 * (size_t)n) * sizeof(double)));
+    double* dA = (double*)h->dense_io.ptr;
+    double *dd = dA + nn, *de = dd + n, *dt = de + n;
+    cudaStream_t st = h->stream;
+    CK(cudaMemcpy2DAsync(dA, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n,
+                         cudaMemcpyHostToDevice, st));
+    rc = symeig_sytrd_f64_dev(h, n, dA, n, dd, de, dt);
+    if (rc) return rc;
+    CK(cudaMemcpy2DAsync(A, lda * sizeof(double), dA, n * sizeof(double), n * sizeof(double), n,
+                         cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(d, dd, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (n > 1) {
+        CK(cudaMemcpyAsync(e, de, (n - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(cudaMemcpyAsync(tau, dt, (n - 1) * sizeof(double), cudaMemcpyDeviceToHost, st));
+    }
+    CK(cudaStreamSynchronize(st));
+    return SYMEIG_OK;
+}
+
+int symeig_orgtr_f64(symeig_handle h, int64_t n, const double* A, int64_t lda, const double* tau,
+                     double* Q, int64_t ldq)
+{
+    int rc = dense_args(h, n, A, lda);
+    if (rc) return rc;
+    if (!Q || (n > 1 && !tau)) return SYMEIG_ERR_NULL;
+    if (ldq < n) return SYMEIG_ERR_LD;
+    const size_t nn = (size_t)n * n;
+    CK(h->dense_io.ensure((2 * nn + (size_t)n) * sizeof(double)));
+    double* dA = (double*)h->dense_io.ptr;
+    double *dQ = dA + nn, *dt = dQ + nn;
+    cudaStream_t st = h->stream;
+    CK(cudaMemcpy2DAsync(dA, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n,
+                         cudaMemcpyHostToDevice, st));
+    if (n > 1) CK(cudaMemcpyAsync(dt, tau, (n - 1) * sizeof(double), cudaMemcpyHostToDevice, st));
+    rc = symeig_orgtr_f64_dev(h, n, dA, n, dt, dQ, n);
+    if (rc) return rc;
+    CK(cudaMemcpy2DAsync(Q, ldq * sizeof(double), dQ, n * sizeof(double), n * sizeof(double), n,
+                         cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    return SYMEIG_OK;
+}
+
+int symeig_syev_f64(symeig_handle h, int64_t n, const double* A, int64_t lda, double* lam, double* V,
+                    int64_t ldv, int32_t* converged, int64_t* iter)
+{
+    int rc = dense_args(h, n, A, lda);
+    if (rc) return rc;
+    if (!lam || !V || !converged || !iter) return SYMEIG_ERR_NULL;
+    if (ldv < n) return SYMEIG_ERR_LD;
+    auto t0 = std::chrono::steady_clock::now();
+    const size_t nn = (size_t)n * n;
+    CK(h->dense_io.ensure((2 * nn + (size_t)n) * sizeof(double)));
+    double* dA = (double*)h->dense_io.ptr;
+    double *dV = dA + nn, *dl = dV + nn;
+    cudaStream_t st = h->stream;
+    CK(cudaMemcpy2DAsync(dA, n * sizeof(double), A, lda * sizeof(double), n * sizeof(double), n,
+                         cudaMemcpyHostToDevice, st));
+    rc = symeig_syev_f64_dev(h, n, dA, n, dl, dV, n, converged, iter);
+    if (rc) return rc;
+    CK(cudaMemcpy2DAsync(V, ldv * sizeof(double), dV, n * sizeof(double), n * sizeof(double), n,
+                         cudaMemcpyDeviceToHost, st));
+    CK(cudaMemcpyAsync(lam, dl, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    h->stats.total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     return SYMEIG_OK;
 }
 

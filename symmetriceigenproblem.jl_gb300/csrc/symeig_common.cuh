@@ -111,6 +111,18 @@ cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t g
 void apply_set_shape(int fp64, int shape);
 int apply_get_shape(int fp64);
 
+// Dense symmetric -> tridiagonal (sytrd.cu).  Scratch sizes in doubles.
+int64_t dense_scratch_doubles(int64_t n);
+int sytrd_dev(cudaStream_t s, int64_t n, double* A, int64_t lda, double* d, double* e, double* tau,
+              double* scratch);
+int orgtr_dev(cudaStream_t s, int64_t n, const double* A, int64_t lda, const double* tau, double* Q,
+              int64_t ldq, double* scratch);
+// max |A_ij| into *out (device), and A *= scale (exact for a power of two)
+cudaError_t launch_dense_maxabs(const double* A, int64_t lda, int64_t n, double* out, cudaStream_t s);
+cudaError_t launch_dense_scale(double* A, int64_t lda, int64_t n, double scale, cudaStream_t s);
+// d *= f, e *= f, and the diagonal / subdiagonal of A set from them
+cudaError_t launch_tridiag_unscale(double* A, int64_t lda, int64_t n, double* d, double* e,
+                                   double f, cudaStream_t s);
 // givensAlgorithm elementwise on device arrays (form 0 Newton form, 1 reference form).
 cudaError_t launch_get_rotation(int64_t count, const double* f, const double* g, double* c,
                                 double* s, double* r, int32_t form, cudaStream_t stream);

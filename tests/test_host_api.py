@@ -102,3 +102,15 @@ def test_oracle_flush_generator(oracle):
             assert thick.max() <= 4 and place.max() >= 1
             assert grid.shape == (n - 1, 8, 2)   # exact-order grids hold 2 * max_layers
     assert statuses[-1] == 0 and all(s == 1 for s in statuses[:-1]) and len(statuses) > 2
+
+
+def test_dense_entry_points_validate_arguments(pkg):
+    """sytrd / orgtr / syev reject bad handles and sizes before touching a device."""
+    lib = pkg.load_library()
+    import ctypes
+    buf = (ctypes.c_double * 16)()
+    c32, c64 = ctypes.c_int32(), ctypes.c_int64()
+    assert lib.symeig_sytrd_f64(None, 4, buf, 4, buf, buf, buf) == 5          # SYMEIG_ERR_HANDLE
+    assert lib.symeig_orgtr_f64(None, 4, buf, 4, buf, buf, 4) == 5
+    assert lib.symeig_syev_f64(None, 4, buf, 4, buf, buf, 4, ctypes.byref(c32), ctypes.byref(c64)) == 5
+    assert lib.symeig_sytrd_f64_dev(None, 4, buf, 4, buf, buf, buf) == 5
