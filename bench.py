@@ -55,6 +55,9 @@ def parse_args():
     p.add_argument("--q", choices=["f64", "f32"], default="f64", help="solve workload: Q precision")
     p.add_argument("--oracle-check", action="store_true",
                    help="solve workload: also run the CPU oracle's chase (eigenvalues only) and compare bits")
+    p.add_argument("--form", choices=["canonical", "scaled"], default="canonical",
+                   help="FP64 apply form: canonical rotations (4 FP64 ops per rotation-row) or the "
+                        "scaled form (2 FMAs per rotation-row; a few ulps from canonical)")
     p.add_argument("--chase-mode", type=int, choices=[0, 1, 2], default=0,
                    help="solve workload: 0 Newton-form two-warp chase, 1 reference form, 2 Newton + redo")
     p.add_argument("--count", type=int, default=4096, help="batched workload: number of tridiagonals")
@@ -220,6 +223,8 @@ def run_ours(args):
     stream = torch.cuda.Stream(dev)
     h.set_stream(stream.cuda_stream)
     h.set_kernel_timing(True)
+    form = 1 if (args.form == "scaled" and args.dtype == "f64") else 0
+    h.set_apply_form(form)
 
     m, n, k = args.m, args.n, args.k
     import ctypes
@@ -248,7 +253,8 @@ def run_ours(args):
             step()
             st = h.stats()   # waits for the step's last wave kernel; per-kernel device time
             kernel_ms.append(st["wave_kernel_ms"] / max(st["wave_launches"], 1))
-            launches += 2 * st["wave_launches"]   # table build + wave kernel per pass
+            # per pass: table build + wave kernel (the scaled form adds the scale recurrence)
+            launches += (3 if form else 2) * st["wave_launches"]
         e1.record(stream)
         torch.cuda.synchronize()
     clocks = clk.summary()
@@ -276,6 +282,7 @@ def run_ours(args):
     hcs.copy_(cs)
     hfn = getattr(lib, f"symeig_apply_givens_{args.dtype}")
     h2 = pkg.Handle(local)
+    h2.set_apply_form(form)
 
     def e2e_step():
         rc = hfn(h2.ptr, ctypes.c_void_p(hq.data_ptr()), m, m, n, ctypes.c_void_p(hcs.data_ptr()), k)
@@ -321,13 +328,19 @@ def run_ours(args):
             "vs_baseline": None, "dtype": args.dtype,
             "data": "synthetic (seeded U[-1,1) Q, (cos t, sin t) rotations, t ~ U[0, 2pi))",
             "config": {"workload": WORKLOAD, "m": m, "n": n, "k": k,
+                       "form": "scaled" if form else "canonical",
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (Q = %.2f GB)" % (m * n * esz / 1e9)},
             "roofline": {"bound": "fp64" if args.dtype == "f64" else "fp32", "achieved": round(achieved, 4),
                          "peak": round(peak, 4), "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
                          "frac_of_givens_ceiling": round(achieved / peak / 0.75, 4),
                          "peak_source": "measured now by symeig_measure_fma_peak (FMA = 2 flops); "
-                                        "a Givens rotation-row is 4 FMA-pipe ops for 6 counted flops, so 0.75 is the ceiling",
+                                        "a Givens rotation-row is 4 FMA-pipe ops for 6 counted flops, so 0.75 is the ceiling"
+                                        + ("; the scaled form spends 2 FMAs per rotation-row, so its ceiling is 1.5 and "
+                                           "fp64_pipe_frac is the measure of pipe use" if form else ""),
+                         "fp64_instr_per_rotation_row": 2 if form else 4,
+                         "fp64_pipe_frac": round((2 if form else 4) * (fl / 6.0 / passes) / (per_launch_ms * 1e-3)
+                                                 / (peak * 1e12 / 2.0), 4),
                          "traffic": read_traffic(), "algorithmic_bytes": algo_bytes,
                          "kernel_ms": round(per_launch_ms, 3)},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
@@ -412,7 +425,8 @@ def run_solve(args):
     torch.cuda.synchronize()
     with ClockSampler(0) as clk:
         t0 = time.perf_counter()
-        _, conv, it = pkg.qr_algorithm_(pkg.SymTridiagonal(td, te), Q, handle=h, chase_mode=args.chase_mode)
+        _, conv, it = pkg.qr_algorithm_(pkg.SymTridiagonal(td, te), Q, handle=h, chase_mode=args.chase_mode,
+                                        apply_form=1 if (args.form == "scaled" and args.q == "f64") else 0)
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
     st = h.stats()
@@ -439,7 +453,7 @@ def run_solve(args):
         "dtype": "f64" if args.q == "f64" else "f64 chase, f32 Q",
         "data": "synthetic (seeded, as in the full-eigensolve configuration)",
         "config": {"workload": "qr_algorithm!(SymTridiagonal(d, e), Q = I)", "n": n, "case": args.case,
-                   "q": args.q, "max_layers": 128, "chase_mode": args.chase_mode},
+                   "q": args.q, "max_layers": 128, "chase_mode": args.chase_mode, "form": args.form},
         "converged": bool(conv), "iterations": it, "rotations": st["rotations"], "flushes": st["flushes"],
         "chase_ms": round(st["chase_ms"], 1), "apply_ms": round(st["apply_ms"], 1),
         "chase_us_per_rotation": round(st["chase_ms"] * 1e3 / max(st["rotations"], 1), 4),

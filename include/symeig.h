@@ -79,6 +79,14 @@ int symeig_set_exact_order(symeig_handle h, int32_t exact_order);
  * 2: as 0, but every sweep is then redone in the reference form (exercises the restore).
  * No reference counterpart. */
 int symeig_set_chase_mode(symeig_handle h, int32_t mode);
+/* Arithmetic form of the FP64 bulk apply (symeig_apply_givens_f64*, and the qr driver's
+ * apply with FP64 Q).  0 (default): every rotation as the reference's rmul!, four FP64
+ * operations per rotation and row.  1: the scaled ("fast Givens") form: columns carry scale
+ * factors within each pass of 64 layers, so a rotation costs two FMAs per row; results agree
+ * with form 0 to a few ulps per rotation (not bit for bit) and with the oracle's restatement
+ * of the same form bit for bit.  The FP32, left, batched and allocation-free applies always
+ * use form 0.  No reference counterpart. */
+int symeig_set_apply_form(symeig_handle h, int32_t form);
 /* Record CUDA events around every wave-kernel launch so symeig_get_stats can report their
  * device time (wave_kernel_ms).  Off by default.  symeig_get_stats waits for the last
  * marked launch.  No reference counterpart (the reference times with BenchmarkTools). */

@@ -53,6 +53,12 @@ def lib():
                                 c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(c_i64),
                                 ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)]
         L.oracle_qr.restype = ctypes.c_int
+        L.oracle_qr_form.argtypes = [c_vp, c_vp, c_i64, c_vp, c_i64, c_i64, ctypes.c_int, c_i32, c_dbl, c_i64,
+                                     c_i32, c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(c_i64),
+                                     ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)]
+        L.oracle_qr_form.restype = ctypes.c_int
+        L.oracle_apply_scaled_f64.argtypes = [c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]
+        L.oracle_apply_scaled_f64.restype = ctypes.c_int
         L.oracle_qr_init.argtypes = [c_vp, c_i64, c_i32, c_dbl, c_i64, c_i32]
         L.oracle_qr_init.restype = None
         L.oracle_qr_flush.argtypes = [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]
@@ -99,6 +105,21 @@ def apply_seq(Q: np.ndarray, cs: np.ndarray) -> None:
     ld = Q.strides[1] // Q.itemsize if n > 1 else max(m, 1)
     fn = lib().oracle_apply_seq_f64 if Q.dtype == np.float64 else lib().oracle_apply_seq_f32
     fn(_ptr(Q), ld, m, n, _ptr(flat), k)
+
+
+def apply_scaled(Q: np.ndarray, cs: np.ndarray) -> None:
+    """The device's scaled (fast-Givens) form of the bulk apply, in place on FP64 Q: passes of
+    64 layers with per-column scale factors (see oracle_apply_scaled_pass_f64)."""
+    _check_q(Q)
+    if Q.dtype != np.float64:
+        raise TypeError("the scaled form is FP64 only")
+    m, n = Q.shape
+    k = cs.shape[1] if cs.ndim == 3 else 0
+    flat = np.ascontiguousarray(np.transpose(cs, (1, 0, 2)).reshape(-1), dtype=np.float64) if k else np.zeros(2)
+    ld = Q.strides[1] // Q.itemsize if n > 1 else max(m, 1)
+    rc = lib().oracle_apply_scaled_f64(_ptr(Q), ld, m, n, _ptr(flat), k)
+    if rc != 0:
+        raise RuntimeError(f"oracle_apply_scaled_f64 failed with status {rc}")
 
 
 def apply_wave(Q: np.ndarray, cs: np.ndarray, nthreads: int = 1) -> None:
@@ -164,11 +185,13 @@ def qr_timeorder(d: np.ndarray, e: np.ndarray, Q: np.ndarray, max_layers: int = 
 
 
 def qr_algorithm(d: np.ndarray, e: np.ndarray, Q: np.ndarray | None, max_layers: int = 128,
-                 tol: float | None = None, maxiter: int | None = None, exact_order: bool = True):
+                 tol: float | None = None, maxiter: int | None = None, exact_order: bool = True,
+                 apply_form: int = 0):
     """qr_algorithm!(SymTridiagonal(d, e), Q, max_layers, tol, maxiter)
     (src/bulge_chasing.jl:146-288): d, e and Q updated in place.  exact_order=False keeps the
     reference's grid placement (rotation i of a sweep at layer ++thickness[i]); True (default)
     places each sweep at one layer so the grid's layer-major order is the chase's order.
+    apply_form=1 applies each flush in the device's scaled form (FP64 Q only).
     Returns (converged, iter, flushes, rotations)."""
     n = d.shape[0]
     assert d.dtype == np.float64 and e.dtype == np.float64 and e.shape[0] == max(n - 1, 0)
@@ -183,8 +206,9 @@ def qr_algorithm(d: np.ndarray, e: np.ndarray, Q: np.ndarray | None, max_layers:
     else:
         m, ld, qp, is32 = 0, 1, None, 0
     ebuf = e if e.size else np.zeros(1)
-    rc = lib().oracle_qr(_ptr(d), _ptr(ebuf), n, qp, ld, m, is32, max_layers, tol, maxiter, int(exact_order),
-                         ctypes.byref(conv), ctypes.byref(it), ctypes.byref(fl), ctypes.byref(rot))
+    rc = lib().oracle_qr_form(_ptr(d), _ptr(ebuf), n, qp, ld, m, is32, max_layers, tol, maxiter, int(exact_order),
+                              int(apply_form), ctypes.byref(conv), ctypes.byref(it), ctypes.byref(fl),
+                              ctypes.byref(rot))
     if rc != 0:
         raise RuntimeError(f"oracle_qr failed with status {rc}")
     return bool(conv.value), it.value, fl.value, rot.value

@@ -116,6 +116,91 @@ static inline void rot_f32(float* x, float* y, float c, float s)
     *y = fmaf(c, b, -sa);
 }
 
+/* Scaled ("fast Givens") form of one pass of the device apply (the GB300 kernel's optional
+ * form; no reference counterpart -- the reference applies (c,s) as rmul! does).  Columns
+ * c0 .. c0+nloc-1 of Q carry scale factors d (1 at the start of the pass), Q = Qt diag(d).
+ * Rotation (r, L), r = 0..nloc-2 local, L = 0..63 of the pass, in layer-major order:
+ *   form 1 (|c| >= |s|): k = s/c,  A = k (d[r+1]/d[r]),  B = -(k (d[r]/d[r+1])),
+ *                        d[r] = c d[r],  d[r+1] = c d[r+1]
+ *   form 2 (|s| >  |c|): k = c/s,  A = k (d[r]/d[r+1]),  B = -(k (d[r+1]/d[r])),
+ *                        d[r] = s d[r+1],  d[r+1] = -(s d[r])
+ * (every operation rounded once, divisions correctly rounded), and on every row
+ *   (u, v) = form 2 ? (y, x) : (x, y);   x = fma(A, v, u);   y = fma(B, u, v).
+ * Layers beyond the grid's (`layers`) are padding with A = B = +0, form 1 (the kernel's
+ * zeroed table slots).  At the end of the pass column c is multiplied by d[c].  place (may
+ * be NULL): layer L of rotation i is (1, 0) unless L < place[i], as for the canonical apply. */
+static void scaled_coeffs(double c, double s, double dr, double dr1, double* A, double* B, int* f2,
+                          double* nr, double* nr1)
+{
+    if (fabs(s) > fabs(c)) {
+        const double k = c / s;
+        *A = k * (dr / dr1);
+        *B = -(k * (dr1 / dr));
+        *nr = s * dr1;
+        *nr1 = -(s * dr);
+        *f2 = 1;
+    } else {
+        const double k = s / c;
+        *A = k * (dr1 / dr);
+        *B = -(k * (dr / dr1));
+        *nr = c * dr;
+        *nr1 = c * dr1;
+        *f2 = 0;
+    }
+}
+
+int oracle_apply_scaled_pass_f64(double* Q, int64_t ldq, int64_t m, const double* grid, int64_t grid_rows,
+                                 const int32_t* place, int64_t c0, int64_t nloc, int64_t L0,
+                                 int64_t layers)
+{
+    if (nloc < 2 || m <= 0) return 0;
+    double* d = (double*)malloc(sizeof(double) * nloc);
+    if (!d) return -2;
+    for (int64_t c = 0; c < nloc; ++c) d[c] = 1.0;
+    for (int64_t L = 0; L < 64; ++L)
+        for (int64_t r = 0; r + 1 < nloc; ++r) {
+            double A = 0.0, B = 0.0;
+            int f2 = 0;
+            if (L < layers) {
+                double c = 1.0, s = 0.0;
+                const int64_t i = c0 + r, LL = L0 + L;
+                if (place == NULL || LL < (int64_t)place[i]) {
+                    c = grid[2 * (i + LL * grid_rows)];
+                    s = grid[2 * (i + LL * grid_rows) + 1];
+                }
+                double nr, nr1;
+                scaled_coeffs(c, s, d[r], d[r + 1], &A, &B, &f2, &nr, &nr1);
+                d[r] = nr;
+                d[r + 1] = nr1;
+            }
+            double* x = Q + (c0 + r) * ldq;
+            double* y = Q + (c0 + r + 1) * ldq;
+            for (int64_t row = 0; row < m; ++row) {
+                const double a = x[row], b = y[row];
+                const double u = f2 ? b : a, v = f2 ? a : b;
+                x[row] = fma(A, v, u);
+                y[row] = fma(B, u, v);
+            }
+        }
+    for (int64_t c = 0; c < nloc; ++c) {
+        double* x = Q + (c0 + c) * ldq;
+        for (int64_t row = 0; row < m; ++row) x[row] = d[c] * x[row];
+    }
+    free(d);
+    return 0;
+}
+
+/* The whole bulk apply in the scaled form: passes of 64 layers over columns 0..n-1. */
+int oracle_apply_scaled_f64(double* Q, int64_t ldq, int64_t m, int64_t n, const double* cs, int64_t k)
+{
+    for (int64_t L0 = 0; L0 < k; L0 += 64) {
+        const int64_t layers = k - L0 < 64 ? k - L0 : 64;
+        const int rc = oracle_apply_scaled_pass_f64(Q, ldq, m, cs, n - 1, NULL, 0, n, L0, layers);
+        if (rc) return rc;
+    }
+    return 0;
+}
+
 /* Layer-major definition of the bulk apply: Q (m x n, column-major, leading dim ldq)
  * times every rotation of the (n-1) x k grid cs (Julia Matrix{Tuple{T,T}} layout: entry
  * (i,L), 0-based, holds c at cs[2*(i + L*(n-1))] and s right after it). */
@@ -389,6 +474,7 @@ typedef struct {
     int64_t total_rotations;    /* all rotations written so far */
     int64_t early_flushes;      /* flushes ended because a sweep's layer exceeded grid_layers */
     int64_t max_place;          /* thickest grid column of the last flush */
+    int64_t min_from, max_to;   /* 1-based column range of the last flush's sweeps */
 } oracle_qr_state;
 
 void oracle_qr_init(oracle_qr_state* st, int64_t n, int32_t max_layers, double tol, int64_t maxiter,
@@ -418,6 +504,8 @@ int oracle_qr_flush(oracle_qr_state* st, double* dv, double* ev, double* givens,
     int did_a_thing = 0;
     int64_t rot_before = st->total_rotations;
     int64_t to = st->last_block_ends_at;
+    st->min_from = n + 1;
+    st->max_to = 0;
     for (;;) {
         if (st->iter > st->maxiter) return -1;
         int64_t from = to;
@@ -441,6 +529,8 @@ int oracle_qr_flush(oracle_qr_state* st, double* dv, double* ev, double* givens,
                 double mu = oracle_wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
                 did_a_thing = 1;
                 oracle_single_shift(dv, ev, n, from, to, mu, givens, rows, thick, place, layer);
+                if (from < st->min_from) st->min_from = from;
+                if (to > st->max_to) st->max_to = to;
                 st->total_rotations += to - from;
                 st->iter += 1;
             }
@@ -460,10 +550,29 @@ int oracle_qr_flush(oracle_qr_state* st, double* dv, double* ev, double* givens,
  * with Q * prod(G).  q_is_f32 != 0 means Q is float and every (c,s) is rounded to float
  * before the update (the FP32-Q variant; the chase stays FP64).  Returns 0 on success,
  * a positive value for bad arguments, -2 for allocation failure. */
+int oracle_qr_form(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
+                   int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
+                   int32_t apply_form, int32_t* converged, int64_t* iter, int64_t* flushes,
+                   int64_t* rotations);
+
 int oracle_qr(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
               int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
               int32_t* converged, int64_t* iter, int64_t* flushes, int64_t* rotations)
 {
+    return oracle_qr_form(d, e, n, Q, ldq, m, q_is_f32, max_layers, tol, maxiter, exact_order, 0,
+                          converged, iter, flushes, rotations);
+}
+
+/* oracle_qr with the bulk apply in the canonical form (apply_form 0) or in the device's
+ * scaled form (apply_form 1, FP64 Q): each flush is applied to the columns its sweeps
+ * touched, min_from-1 .. max_to-1, in passes of 64 layers (oracle_apply_scaled_pass_f64),
+ * as the device applies it. */
+int oracle_qr_form(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
+                   int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
+                   int32_t apply_form, int32_t* converged, int64_t* iter, int64_t* flushes,
+                   int64_t* rotations)
+{
+    if (apply_form != 0 && q_is_f32) return 1;
     if (n < 1 || max_layers < 1 || (Q && ldq < m)) return 1;
     oracle_qr_state st;
     oracle_qr_init(&st, n, max_layers, tol, maxiter, exact_order);
@@ -486,6 +595,13 @@ int oracle_qr(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, 
             if (q_is_f32) {
                 for (int64_t q = 0; q < 2 * (n - 1) * K; ++q) g32[q] = (float)givens[q];
                 oracle_apply_seq_f32((float*)Q, ldq, m, n, g32, K);
+            } else if (apply_form == 1) {
+                const int64_t c_lo = st.min_from - 1, n_loc = st.max_to - c_lo;
+                for (int64_t L0 = 0; L0 < K; L0 += 64) {
+                    rc = oracle_apply_scaled_pass_f64((double*)Q, ldq, m, givens, nr, NULL, c_lo, n_loc,
+                                                      L0, K - L0 < 64 ? K - L0 : 64);
+                    if (rc) { free(givens); free(g32); free(thick); free(place); return rc; }
+                }
             } else {
                 oracle_apply_seq_f64((double*)Q, ldq, m, n, givens, K);
             }

@@ -33,6 +33,7 @@ SIGNATURES = {
     "symeig_get_stats": (ctypes.c_int, [c_vp, c_vp]),
     "symeig_set_exact_order": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_chase_mode": (ctypes.c_int, [c_vp, c_i32]),
+    "symeig_set_apply_form": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_get_rotation_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "symeig_sytrd_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "symeig_sytrd_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp]),
@@ -153,6 +154,10 @@ class Handle:
 
     def set_exact_order(self, exact: bool):
         check("symeig_set_exact_order", self._lib.symeig_set_exact_order(self.ptr, int(bool(exact))))
+
+    def set_apply_form(self, form):
+        """0: canonical rotations (default); 1: the scaled form for FP64 applies."""
+        check("symeig_set_apply_form", self._lib.symeig_set_apply_form(self.ptr, int(form)))
 
     def set_chase_mode(self, mode):
         """0: Newton-form two-warp chase (default); 1: reference form; 2: Newton form with

@@ -147,9 +147,11 @@ def _givens_ptr(givens, dtype_name: str, on_device: bool):
     return buf.ctypes.data, buf, int(g.shape[1])
 
 
-def bulk_wave_order_2x2_rmul_(A, givens, handle: Handle | None = None) -> None:
+def bulk_wave_order_2x2_rmul_(A, givens, handle: Handle | None = None, form: int = 0) -> None:
     """A <- A * prod(G) for the (n-1) x k rotation grid, in the reference's wave order
-    (src/wave.jl:62-162).  Unlike the reference, any n and any k are accepted."""
+    (src/wave.jl:62-162).  Unlike the reference, any n and any k are accepted.  form=1 uses
+    the scaled (fast-Givens) form for FP64 A (symeig_set_apply_form): two FMAs per rotation
+    and row, a few ulps from form 0."""
     ptr, ld, m, n, dt, dev = _colmajor_info(A)
     gn = int(givens.shape[0])
     if n >= 2 and gn != n - 1:
@@ -159,11 +161,15 @@ def bulk_wave_order_2x2_rmul_(A, givens, handle: Handle | None = None) -> None:
     h = handle or default_handle(A.device.index if _is_torch(A) else 0)
     gptr, keep, k = _givens_ptr(givens, dt, dev)
     name = f"symeig_apply_givens_{dt}" + ("_dev" if dev else "")
-    if dev:  # run on torch's current stream: ordered after the producers of A and givens
-        with h.on_stream(torch.cuda.current_stream(A.device).cuda_stream):
+    h.set_apply_form(form)
+    try:
+        if dev:  # run on torch's current stream: ordered after the producers of A and givens
+            with h.on_stream(torch.cuda.current_stream(A.device).cuda_stream):
+                h.call(name, ctypes.c_void_p(ptr), ld, m, n, ctypes.c_void_p(gptr), k)
+        else:
             h.call(name, ctypes.c_void_p(ptr), ld, m, n, ctypes.c_void_p(gptr), k)
-    else:
-        h.call(name, ctypes.c_void_p(ptr), ld, m, n, ctypes.c_void_p(gptr), k)
+    finally:
+        h.set_apply_form(0)
     if dev:
         # keep the temporary Julia-layout copy alive until the kernels that read it finish
         torch.cuda.current_stream(A.device).synchronize()
@@ -171,15 +177,15 @@ def bulk_wave_order_2x2_rmul_(A, givens, handle: Handle | None = None) -> None:
     return None
 
 
-def bulk_wave_order_2x2_rmul_parallel_(A, givens, handle: Handle | None = None) -> None:
+def bulk_wave_order_2x2_rmul_parallel_(A, givens, handle: Handle | None = None, form: int = 0) -> None:
     """src/wave.jl:36-60: the row-slab threaded variant.  On the GPU every row already has
     its own thread, so this is the same call."""
-    return bulk_wave_order_2x2_rmul_(A, givens, handle)
+    return bulk_wave_order_2x2_rmul_(A, givens, handle, form)
 
 
 def qr_algorithm_(H: SymTridiagonal, Q=None, max_layers: int = 128, tol: float | None = None,
                   maxiter: int | None = None, handle: Handle | None = None,
-                  exact_order: bool = True, chase_mode: int = 0):
+                  exact_order: bool = True, chase_mode: int = 0, apply_form: int = 0):
     """qr_algorithm!(H, Q, max_layers=128, tol=eps(T), maxiter=100n) -> (H, converged, iter)
     (src/bulge_chasing.jl:146-288).  H.dv becomes the (unsorted) eigenvalues, Q <- Q*prod(G).
     Q may be None (eigenvalues only), float64 or float32 (the FP32-Q variant: FP64 chase,
@@ -187,7 +193,8 @@ def qr_algorithm_(H: SymTridiagonal, Q=None, max_layers: int = 128, tol: float |
     does (grid[i, ++layer_thickness[i]]), which loses accuracy in Q when a split block
     re-merges within a flush; the default places each sweep at one layer so Q is exact.
     chase_mode selects how the chase computes rotations (symeig_set_chase_mode); every mode
-    gives the same bits."""
+    gives the same bits.  apply_form=1 applies each flush to an FP64 Q in the scaled form
+    (symeig_set_apply_form)."""
     n = H.n
     tol = EPS64 if tol is None else float(tol)
     maxiter = 100 * n if maxiter is None else int(maxiter)
@@ -218,6 +225,7 @@ def qr_algorithm_(H: SymTridiagonal, Q=None, max_layers: int = 128, tol: float |
     name = "symeig_qr_f64" + ("_q32" if dt == "f32" else "") + ("_dev" if dev else "")
     h.set_exact_order(exact_order)
     h.set_chase_mode(chase_mode)
+    h.set_apply_form(apply_form)
     try:
         args = (ctypes.c_void_p(dptr), ctypes.c_void_p(eptr), n, ctypes.c_void_p(qptr), ld, m,
                 int(max_layers), tol, maxiter, ctypes.byref(conv), ctypes.byref(it))
@@ -229,6 +237,7 @@ def qr_algorithm_(H: SymTridiagonal, Q=None, max_layers: int = 128, tol: float |
     finally:
         h.set_exact_order(True)
         h.set_chase_mode(0)
+        h.set_apply_form(0)
     return H, bool(conv.value), int(it.value)
 
 

@@ -59,6 +59,7 @@ struct symeig_context {
     int* derr = nullptr;   // device error word of the wave kernels (bounded waits)
     int32_t exact_order = 1;  // rotation placement of the qr driver
     int32_t chase_mode = 0;   // symeig_set_chase_mode
+    int32_t apply_form = 0;   // symeig_set_apply_form
     ChaseState* h_state = nullptr;  // pinned
     std::vector<cudaEvent_t> timing;  // pool of timing events
     symeig_stats stats{};
@@ -145,6 +146,7 @@ int apply_grid(symeig_handle h, T* Q, int64_t ldq, int64_t m, const Tsrc* grid, 
     CK(h->table.ensure(apply_table_bytes<T>(n_loc, per)));
     for (int64_t L0 = 0; L0 < layers; L0 += per) {
         ApplyPass pass{c0, n_loc, L0, std::min(per, layers - L0), rs};
+        pass.form = sizeof(T) == 8 ? h->apply_form : 0;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (h->kernel_timing) {
             e0 = kernel_event(h);
@@ -569,6 +571,14 @@ int symeig_set_chase_mode(symeig_handle h, int32_t mode)
     if (!h) return SYMEIG_ERR_HANDLE;
     if (mode < 0 || mode > 2) return SYMEIG_ERR_SIZE;
     h->chase_mode = mode;
+    return SYMEIG_OK;
+}
+
+int symeig_set_apply_form(symeig_handle h, int32_t form)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    if (form < 0 || form > 1) return SYMEIG_ERR_SIZE;
+    h->apply_form = form;
     return SYMEIG_OK;
 }
 

@@ -55,7 +55,192 @@ build_table_kernel(unsigned char* __restrict__ table, int64_t n_chunks,
     }
 }
 
-template <typename T, int S>
+// ---- the scaled (fast-Givens) form, FP64 -----------------------------------------------
+//
+// With Q = Qt diag(d) (d = 1 at the start of a pass), rotation (r, L) of the pass becomes two
+// FMAs per row of Qt (wave_rotations_scaled):
+//   form 1 (|c| >= |s|): k = s/c,  A = k (d[r+1]/d[r]),  B = -(k (d[r]/d[r+1])),
+//                        d[r] <- c d[r],  d[r+1] <- c d[r+1];
+//   form 2 (|s| >  |c|): k = c/s,  A = k (d[r]/d[r+1]),  B = -(k (d[r+1]/d[r])),
+//                        d[r] <- s d[r+1],  d[r+1] <- -(s d[r]),
+// each operation rounded once (divisions correctly rounded), and column c is multiplied by
+// its final d[c] when it is stored.  |A B| <= 1 and every d loses at most a factor sqrt(2) per
+// rotation, so 64 layers keep d within [2^-64, 1]; the error per rotation is of the order of
+// the canonical form's (a few ulps).  Two kernels build the table:
+//   scaled_recurrence_kernel: the d recurrence itself.  Only the multiplications d <- c d
+//     form the chain; it runs as a wavefront (rotations r + 2L = step are independent and
+//     touch disjoint columns) on one CTA of one thread per layer, and records each
+//     rotation's d[r], d[r+1] before it, its form, and each column's final d.
+//   scaled_table_kernel: A and B of every slot from those (the divisions, all independent),
+//     the group's flag word and, for group G-1, the final d of the column it stores.
+
+constexpr int kRB = 64;   // recurrence steps per staging block
+constexpr int kPL = 2 * 63 + kRB;  // columns whose place[] a staging block needs
+
+// shared memory of the recurrence: two staging blocks of (c, s) (one row of kRB pairs per
+// layer) and of place[], and the ring of column scales
+struct RecSmem {
+    double2 cs[2][64][kRB + 1];   // rows padded by one pair: thread L reads row L
+    int32_t pl[2][kPL + 2];
+    double d[256];
+};
+
+template <typename Tsrc>
+__device__ __forceinline__ double2 grid_cs(const Tsrc* grid, int64_t grid_rows, const int32_t* place,
+                                           int64_t i, int64_t L)
+{
+    if (place != nullptr && L >= (int64_t)place[i]) return make_double2(1.0, 0.0);
+    const Tsrc* p = grid + 2 * (i + L * grid_rows);
+    return make_double2((double)p[0], (double)p[1]);
+}
+
+__device__ __forceinline__ void cp_async16(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(wave::smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(wave::smem_u32(dst)), "l"(src) : "memory");
+}
+
+// Stage block `blk` (steps [blk kRB, (blk+1) kRB)): thread L copies its rotations
+// r = t - 2L of those steps (layer L0+L, contiguous in the grid), all threads together the
+// place[] entries of columns [blk kRB - 126, blk kRB + kRB).
+__device__ __forceinline__ void rec_stage(RecSmem& sm, int buf, int64_t blk, const double* grid,
+                                          int64_t grid_rows, const int32_t* place, int64_t c0,
+                                          int64_t nr, int64_t L0, int64_t layers)
+{
+    const int L = threadIdx.x;
+    const int64_t T = blk * kRB;
+    if (L < layers) {
+        const int64_t r0 = T - 2 * L;
+        for (int k = 0; k < kRB; ++k) {
+            const int64_t r = r0 + k;
+            if (r >= 0 && r < nr) cp_async16(&sm.cs[buf][L][k], grid + 2 * (c0 + r + (L0 + L) * grid_rows));
+        }
+    }
+    if (place != nullptr) {
+        for (int q = L; q < kPL; q += 64) {
+            const int64_t r = T - 126 + q;
+            if (r >= 0 && r < nr) cp_async4(&sm.pl[buf][q], place + c0 + r);
+        }
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+// The d recurrence of one pass (see the section comment); one CTA of 64 threads, thread L =
+// layer L of the pass; step t treats rotation (t - 2L, L).  The grid is FP64 (the scaled
+// form is FP64 only).
+__global__ void __launch_bounds__(64)
+scaled_recurrence_kernel(const double* __restrict__ grid, int64_t grid_rows,
+                         const int32_t* __restrict__ place, int64_t c0, int64_t n_loc, int64_t L0,
+                         int64_t layers, double2* __restrict__ pre, unsigned char* __restrict__ form,
+                         double* __restrict__ dfinal)
+{
+    extern __shared__ __align__(16) unsigned char rec_raw[];
+    RecSmem& sm = *reinterpret_cast<RecSmem*>(rec_raw);
+    const int L = threadIdx.x;
+    const int64_t nr = n_loc - 1;                       // rotations per layer
+    const int64_t last = nr - 1 + 2 * (layers - 1);     // last step
+    const int64_t nblk = last / kRB + 1;
+    const bool active = L < layers;
+    if (threadIdx.x == 0) sm.d[0] = 1.0;
+    rec_stage(sm, 0, 0, grid, grid_rows, place, c0, nr, L0, layers);
+    for (int64_t blk = 0; blk < nblk; ++blk) {
+        const int buf = (int)(blk & 1);
+        if (blk + 1 < nblk) {
+            rec_stage(sm, buf ^ 1, blk + 1, grid, grid_rows, place, c0, nr, L0, layers);
+            asm volatile("cp.async.wait_group 1;" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;" ::: "memory");
+        }
+        __syncthreads();
+        const int64_t T = blk * kRB;
+        for (int k = 0; k < kRB; ++k) {
+            const int64_t t = T + k;
+            if (t > last) break;   // uniform
+            // column t+1 is first touched at step t (rotation (t, 0), thread 0)
+            if (threadIdx.x == 0 && t + 1 < n_loc) sm.d[(t + 1) & 255] = 1.0;
+            const int64_t r = t - 2 * L;
+            if (active && r >= 0 && r < nr) {
+                double2 cs = sm.cs[buf][L][k];
+                if (place != nullptr && L0 + L >= (int64_t)sm.pl[buf][r - (T - 126)]) cs = make_double2(1.0, 0.0);
+                const double c = cs.x, s = cs.y;
+                const double dr = sm.d[r & 255], dr1 = sm.d[(r + 1) & 255];
+                // |s| > |c| on the integer pipe (an FP64 compare costs an FP64 issue slot)
+                const uint64_t ac = (uint64_t)__double_as_longlong(c) & 0x7FFFFFFFFFFFFFFFull;
+                const uint64_t as = (uint64_t)__double_as_longlong(s) & 0x7FFFFFFFFFFFFFFFull;
+                const bool f2 = as > ac;
+                pre[L * nr + r] = make_double2(dr, dr1);
+                form[L * nr + r] = f2 ? 1 : 0;
+                // form 1: (c dr, c dr1); form 2: (s dr1, -(s dr)) = (s dr1, (-s) dr)
+                const double ns = __longlong_as_double(__double_as_longlong(s) ^ (long long)0x8000000000000000ull);
+                const double m1 = f2 ? s : c, m2 = f2 ? ns : c;
+                const double x1 = f2 ? dr1 : dr, x2 = f2 ? dr : dr1;
+                sm.d[r & 255] = m1 * x1;
+                sm.d[(r + 1) & 255] = m2 * x2;
+            }
+            __syncthreads();
+            // column t - 2 (layers - 1) had its last rotation at this step (and the last
+            // column with it)
+            const int64_t cf = t - 2 * (layers - 1);
+            if (threadIdx.x == 0 && cf >= 0 && cf < nr) {
+                dfinal[cf] = sm.d[cf & 255];
+                if (cf == nr - 1) dfinal[cf + 1] = sm.d[(cf + 1) & 255];
+            }
+        }
+        __syncthreads();   // the staging buffer of this block is refilled next
+    }
+}
+
+template <typename Tsrc, int S>
+__global__ void __launch_bounds__(256)
+scaled_table_kernel(unsigned char* __restrict__ table, int64_t n_chunks, const Tsrc* __restrict__ grid,
+                    int64_t grid_rows, const int32_t* __restrict__ place, int64_t c0, int64_t n_loc,
+                    int64_t L0, int64_t layers, const double2* __restrict__ pre,
+                    const unsigned char* __restrict__ form, const double* __restrict__ dfinal)
+{
+    using Sh = typename Cfg<double, S>::Sh;
+    constexpr int KB = Sh::KB, G = Sh::G, W = Sh::W;
+    const int64_t nr = n_loc - 1;
+    const int64_t total = n_chunks * Sh::CH * G;
+    for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t t = idx / G;
+        const int g = (int)(idx % G);
+        unsigned char* base = table + t * Sh::ITER + g * Sh::GSTRIDE;
+        uint32_t flags = 0;
+#pragma unroll
+        for (int l = 0; l < KB; ++l) {
+            const int64_t i_loc = t - (int64_t)g * W - 1 - l;
+            const int64_t lay = (int64_t)g * KB + l;
+            double A = 0.0, B = 0.0;
+            if (i_loc >= 0 && i_loc < nr && lay < layers) {
+                const double2 cs = grid_cs(grid, grid_rows, place, c0 + i_loc, L0 + lay);
+                const double2 p = pre[lay * nr + i_loc];
+                if (form[lay * nr + i_loc]) {
+                    const double k = cs.x / cs.y;
+                    A = k * (p.x / p.y);
+                    B = -(k * (p.y / p.x));
+                    flags |= 1u << l;
+                } else {
+                    const double k = cs.y / cs.x;
+                    A = k * (p.y / p.x);
+                    B = -(k * (p.x / p.y));
+                }
+            }
+            *reinterpret_cast<double2*>(base + l * 16) = make_double2(A, B);
+        }
+        double dst = 0.0;
+        const int64_t cst = t - (int64_t)(G - 1) * W - KB;   // the column group G-1 stores
+        if (g == G - 1 && cst >= 0 && cst < n_loc) dst = dfinal[cst];
+        *reinterpret_cast<uint32_t*>(base + KB * 16) = flags;
+        *reinterpret_cast<uint32_t*>(base + KB * 16 + 4) = 0u;
+        *reinterpret_cast<double*>(base + KB * 16 + 8) = dst;
+    }
+}
+
+template <typename T, int S, bool SCALED = false>
 __global__ void __launch_bounds__(kThreads, Cfg<T, S>::MINB)
 wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
                   const unsigned char* __restrict__ table, int32_t n_chunks, int* __restrict__ err,
@@ -67,7 +252,7 @@ wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
     wave::Staging<Sh> st{ring, bar, 0, 0};
     wave::staging_init(st);
     const int64_t row0 = (int64_t)blockIdx.x * Sh::ROWS;
-    if (!wave::wave_tile<T, Sh>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs)) {
+    if (!wave::wave_tile<T, Sh, SCALED>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs)) {
         if (threadIdx.x == 0) atomicExch(err, 1);
     }
 }
@@ -78,14 +263,33 @@ template <typename T> int64_t apply_layers_per_pass() { return 64; }
 template int64_t apply_layers_per_pass<double>();
 template int64_t apply_layers_per_pass<float>();
 
+// bytes of the larger of the two shapes' tables (so the tuning can change between calls),
+// rounded up to 256
+template <typename T> size_t table_region(int64_t n_loc)
+{
+    const size_t b = (size_t)std::max(Cfg<T, 0>::Sh::table_bytes(n_loc), Cfg<T, 1>::Sh::table_bytes(n_loc));
+    return (b + 255) & ~(size_t)255;
+}
+
+// the scaled form's scratch after the table: pre (64 x (n_loc-1) double2), form (64 x
+// (n_loc-1) bytes, padded), dfinal (n_loc doubles)
+inline size_t scaled_pre_bytes(int64_t n_loc) { return (size_t)64 * (size_t)(n_loc - 1) * 16; }
+inline size_t scaled_form_bytes(int64_t n_loc) { return ((size_t)64 * (size_t)(n_loc - 1) + 255) & ~(size_t)255; }
+
 template <typename T> size_t apply_table_bytes(int64_t n_loc, int64_t layers)
 {
     (void)layers;
-    // the larger of the two shapes' tables, so the tuning can change between calls
-    return (size_t)std::max(Cfg<T, 0>::Sh::table_bytes(n_loc), Cfg<T, 1>::Sh::table_bytes(n_loc));
+    size_t b = table_region<T>(n_loc);
+    if (sizeof(T) == 8 && n_loc >= 2)
+        b += scaled_pre_bytes(n_loc) + scaled_form_bytes(n_loc) + (size_t)n_loc * sizeof(double);
+    return b;
 }
 template size_t apply_table_bytes<double>(int64_t, int64_t);
 template size_t apply_table_bytes<float>(int64_t, int64_t);
+
+template <typename T> size_t apply_canonical_table_bytes(int64_t n_loc) { return table_region<T>(n_loc); }
+template size_t apply_canonical_table_bytes<double>(int64_t);
+template size_t apply_canonical_table_bytes<float>(int64_t);
 
 template <typename Tsrc, typename T, int S>
 cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t grid_rows,
@@ -95,15 +299,45 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
     using Sh = typename Cfg<T, S>::Sh;
     if (m <= 0 || pass.n_loc < 2 || pass.layers <= 0) return cudaSuccess;
     const int64_t n_chunks = Sh::chunks(pass.n_loc);
+    const int64_t blocks = (m + Sh::ROWS - 1) / Sh::ROWS;
+    cudaError_t e;
+    if constexpr (sizeof(T) == 8) {
+        if (pass.form == 1) {
+            unsigned char* tb = (unsigned char*)table;
+            double2* pre = (double2*)(tb + table_region<T>(pass.n_loc));
+            unsigned char* form = (unsigned char*)pre + scaled_pre_bytes(pass.n_loc);
+            double* dfinal = (double*)(form + scaled_form_bytes(pass.n_loc));
+            static_assert(sizeof(Tsrc) == 8, "the scaled form reads an FP64 grid");
+            e = cudaFuncSetAttribute(scaled_recurrence_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(RecSmem));
+            if (e != cudaSuccess) return e;
+            scaled_recurrence_kernel<<<1, 64, sizeof(RecSmem), stream>>>(
+                (const double*)grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers, pre, form, dfinal);
+            const int64_t total = n_chunks * Sh::CH * Sh::G;
+            int64_t tb_blocks = (total + 255) / 256;
+            if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;
+            scaled_table_kernel<Tsrc, S><<<(unsigned)tb_blocks, 256, 0, stream>>>(
+                tb, n_chunks, grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers,
+                pre, form, dfinal);
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+            if (ev_begin) cudaEventRecord(ev_begin, stream);
+            wave_apply_kernel<T, S, true><<<(unsigned)blocks, kThreads, 0, stream>>>(
+                Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
+                (int32_t)n_chunks, err, (T)-0.0, pass.rs);
+            e = cudaGetLastError();
+            if (ev_end) cudaEventRecord(ev_end, stream);
+            return e;
+        }
+    }
     const int64_t total = n_chunks * Sh::CH * Sh::G * Sh::KB;
     int64_t tb_blocks = (total + 255) / 256;
     if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;
     build_table_kernel<Tsrc, T, S><<<(unsigned)tb_blocks, 256, 0, stream>>>(
         (unsigned char*)table, n_chunks, grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0,
         pass.layers);
-    cudaError_t e = cudaGetLastError();
+    e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    const int64_t blocks = (m + Sh::ROWS - 1) / Sh::ROWS;
     if (ev_begin) cudaEventRecord(ev_begin, stream);
     wave_apply_kernel<T, S><<<(unsigned)blocks, kThreads, 0, stream>>>(
         Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,

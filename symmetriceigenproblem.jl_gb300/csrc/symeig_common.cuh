@@ -85,13 +85,16 @@ struct ChaseState {
 struct ApplyPass {
     int64_t c0, n_loc, L0, layers;
     int64_t rs = 1;  // stride between the kernel's rows (1: rmul!, lda: lmul! on the transpose)
+    int32_t form = 0;  // 0 canonical rotations, 1 the scaled form (FP64 only; see apply.cu)
 };
 
 // Layers one pass of the wave-window kernel handles for element type T.
 template <typename T> int64_t apply_layers_per_pass();
 
-// Bytes of the wave table one pass needs.
+// Bytes of the wave table one pass needs (for FP64 including the scaled form's scratch).
 template <typename T> size_t apply_table_bytes(int64_t n_loc, int64_t layers);
+// Bytes of the canonical form's table alone.
+template <typename T> size_t apply_canonical_table_bytes(int64_t n_loc);
 
 // Build the wave table of one pass from a grid of (c,s) pairs in Julia layout
 // (grid_rows rows, column L = layer L).  When place != nullptr, layer L of rotation i is

@@ -26,6 +26,10 @@
 // tracked by one mbarrier per slot.  Every wait is bounded: after ~2 s of SM clock the tile
 // gives up and reports failure, and the kernel returns without touching Q again.
 //
+// Scaled form (SCALED = true, FP64).  The table holds per slot (A, B) instead of (c, s), the
+// group's form flags in its pad word, and in group G-1's pad the scale factor of the column
+// that group stores in that iteration (see wave_rotations_scaled and apply.cu).
+//
 // Register window.  CH is a multiple of KB+1 and the chunk loop is fully unrolled, so column
 // t always lives in window slot t mod (KB+1), a compile-time constant: the window rotates
 // without register moves.  Group 0 keeps a second ring of KB+1 registers with the next
@@ -163,6 +167,29 @@ __device__ __forceinline__ void wave_rotations(T (&win)[KB + 1], const unsigned 
     }
 }
 
+// The scaled form of the KB rotations of one wave (FP64): each slot holds (A, B) and the
+// group's flag word (in the 16-byte pad after its KB pairs) selects, per slot l, form 2 (bit
+// l set) or form 1.  With (u, v) = form 2 ? (y, x) : (x, y):  x = fma(A, v, u), y = fma(B, u, v)
+// -- two FP64 instructions per rotation-row instead of four.  The scale factors the form
+// folds out of the columns are applied once per pass when group G-1 stores a column.
+template <int KB>
+__device__ __forceinline__ void wave_rotations_scaled(double (&win)[KB + 1], const unsigned char* cs,
+                                                      const int U)
+{
+    constexpr int W = KB + 1;
+    const uint32_t flags = *reinterpret_cast<const uint32_t*>(cs + KB * 16);
+#pragma unroll
+    for (int l = 0; l < KB; ++l) {
+        const double2 p = *reinterpret_cast<const double2*>(cs + l * 16);
+        double& x = win[(U - 1 - l + 2 * W) % W];
+        double& y = win[(U - l + 2 * W) % W];
+        const bool f2 = (flags >> l) & 1u;
+        const double u = f2 ? y : x, v = f2 ? x : y;
+        x = __fma_rn(p.x, v, u);
+        y = __fma_rn(p.y, u, v);
+    }
+}
+
 // CTA-shared staging state of the tile loop: the two-slot ring and one mbarrier per slot,
 // with the number of completed waits per slot (their parity is the phase to wait for next).
 template <typename Sh>
@@ -190,7 +217,7 @@ __device__ __forceinline__ void staging_init(Staging<Sh>& st)
 // the column rotations of rmul! on a column-major matrix, rs = lda and ldq = 1 for the row
 // rotations of lmul! (the same wave on the transposed view).  Every thread of the CTA calls
 // it.  Returns false (all threads) when a bounded wait gave up.
-template <typename T, typename Sh>
+template <typename T, typename Sh, bool SCALED = false>
 __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_t m, int64_t row0,
                                           int32_t n_loc, const unsigned char* __restrict__ table,
                                           int32_t n_chunks, const T nz, Staging<Sh>& st,
@@ -244,9 +271,15 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
                 ahead[u % W] = *lp;
                 lp += ldq;
                 win[u % W] = xin;
-                wave_rotations<T, KB>(win, sb + u * Sh::ITER, u % W, nz);
+                if constexpr (SCALED) wave_rotations_scaled<KB>(win, sb + u * Sh::ITER, u % W);
+                else wave_rotations<T, KB>(win, sb + u * Sh::ITER, u % W, nz);
                 xout = win[(u + 1) % W];
-                if (storer) *sp = xout;
+                if constexpr (SCALED) {
+                    const T dsc = *reinterpret_cast<const T*>(sb + u * Sh::ITER + KB * 16 + 8);
+                    if (storer) *sp = xout * dsc;
+                } else {
+                    if (storer) *sp = xout;
+                }
                 sp += ldq;
             }
         } else {
@@ -261,9 +294,12 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
                 if (u < ld_cnt) nxt = ld_base[(int64_t)u * ldq];
                 ahead[u % W] = nxt;
                 win[u % W] = xin;
-                wave_rotations<T, KB>(win, sb + u * Sh::ITER, u % W, nz);
+                if constexpr (SCALED) wave_rotations_scaled<KB>(win, sb + u * Sh::ITER, u % W);
+                else wave_rotations<T, KB>(win, sb + u * Sh::ITER, u % W, nz);
                 xout = win[(u + 1) % W];
-                st_pred(st_base + (int64_t)u * ldq, xout, storer && u >= st_lo && u < st_hi);
+                T xs = xout;
+                if constexpr (SCALED) xs = xout * *reinterpret_cast<const T*>(sb + u * Sh::ITER + KB * 16 + 8);
+                st_pred(st_base + (int64_t)u * ldq, xs, storer && u >= st_lo && u < st_hi);
             }
         }
         __syncthreads();
