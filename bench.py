@@ -376,6 +376,31 @@ def side_measurements(pkg, lib, h, dev, stream, args):
         out["f32_apply"] = {"value": round(gf, 1), "unit": "GFLOP/s", "ms_per_step": round(ms, 3),
                             "frac_of_fp32_peak": round(gf / 1e3 / peak32, 4), "fp32_peak_tflops": round(peak32, 2)}
         del Q, cs
+    # the scaled (fast-Givens) form of the FP64 apply on the same workload
+    if args.dtype == "f64" and args.form != "scaled":
+        Q, cs = make_inputs(m, n, k, "f64", seed=77, device=dev)
+        fn = lib.symeig_apply_givens_f64_dev
+        h.set_apply_form(1)
+        step = lambda: fn(h.ptr, ctypes.c_void_p(Q.data_ptr()), Q.stride(1), m, n, ctypes.c_void_p(cs.data_ptr()), k)
+        for _ in range(3):
+            step()
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(5):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        st = h.stats()
+        h.set_apply_form(0)
+        ms = e0.elapsed_time(e1) / 5
+        gf = flops_per_step(m, n, k) / (ms * 1e-3) / 1e9
+        peak64 = pkg._lib.measure_fma_peak(dev.index, fp64=True)
+        out["scaled_form"] = {"value": round(gf, 1), "unit": "GFLOP/s", "ms_per_step": round(ms, 3),
+                              "kernel_ms": round(st["wave_kernel_ms"] / max(st["wave_launches"], 1), 3),
+                              "frac_of_fp64_peak": round(gf / 1e3 / peak64, 4),
+                              "note": "two FMAs per rotation-row with per-column scales (symeig_set_apply_form 1); "
+                                      "a few ulps from the canonical form, not bit-equal to it"}
+        del Q, cs
     # qr_algorithm! at n = 2000, d = 1:n, e ~ U[0,1) seed 0 (README.md:65-77)
     nn = 2000
     rng = np.random.default_rng(0)

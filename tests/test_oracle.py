@@ -126,3 +126,38 @@ def test_exact_order_equals_time_order(oracle, n, seed):
     assert np.array_equal(res["exact"][0], res["time"][0])
     assert np.array_equal(res["exact"][1], res["time"][1])
     assert not np.array_equal(res["ref"][1], res["time"][1])
+
+
+def test_oracle_scaled_apply_close_to_canonical(oracle, pkg):
+    """The scaled (fast-Givens) restatement agrees with the canonical rotations to a few ulps
+    per rotation, over several 64-layer passes, and keeps Q orthogonal."""
+    rng = np.random.default_rng(3)
+    for m, n, k in [(40, 33, 10), (64, 65, 64), (90, 130, 150)]:
+        Q0 = np.linalg.qr(rng.standard_normal((n, n)))[0][:m].copy(order="F")
+        th = rng.random((n - 1, k)) * 2 * np.pi
+        cs = pkg.givens_buffer(n - 1, k)
+        cs[..., 0], cs[..., 1] = np.cos(th), np.sin(th)
+        A, B = Q0.copy(order="F"), Q0.copy(order="F")
+        oracle.apply_seq(A, cs)
+        oracle.apply_scaled(B, cs)
+        assert np.max(np.abs(A - B)) <= 8 * (2 * k) * np.finfo(np.float64).eps
+        if m == n:
+            assert np.linalg.norm(B.T @ B - np.eye(n)) <= 10 * n * np.finfo(np.float64).eps
+
+
+def test_oracle_qr_scaled_apply_bounds(oracle):
+    """qr_algorithm! with the scaled apply: the chase is unchanged (eigenvalues bit-equal to the
+    canonical run) and Q meets the residual / orthogonality bounds."""
+    n = 200
+    rng = np.random.default_rng(8)
+    d, e = rng.random(n), rng.random(n - 1)
+    a = (d.copy(), e.copy(), np.asfortranarray(np.eye(n)))
+    b = (d.copy(), e.copy(), np.asfortranarray(np.eye(n)))
+    ra = oracle.qr_algorithm(*a)
+    rb = oracle.qr_algorithm(*b, apply_form=1)
+    assert ra == rb and np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    T = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    eps = np.finfo(np.float64).eps
+    Q, lam = b[2], b[0]
+    assert np.linalg.norm(T @ Q - Q * lam) / np.linalg.norm(T) <= 10 * n * eps
+    assert np.linalg.norm(Q.T @ Q - np.eye(n)) <= 10 * n * eps
