@@ -40,7 +40,13 @@
  * Parity status: the eigenvalues are pinned against LAPACK (the reference test's own check,
  * test/runtests.jl:10) and against the README residual magnitude (README.md:65-77).  The
  * (c,s) stream and Q bits have no golden vectors in the reference (Julia is not available
- * here), so at that boundary the oracle is unpinned.
+ * here); they are pinned against an independent pure-Python restatement with exactly
+ * rounded FMAs (tests/golden/make_golden.py and its fixtures), not against the reference's
+ * own execution.
+ *
+ *   apply (scaled)      The device's optional scaled ("fast Givens") form of the FP64 apply
+ *                       (no reference counterpart), restated so that its results can be
+ *                       checked bit for bit as well.
  */
 #include <math.h>
 #include <stdint.h>

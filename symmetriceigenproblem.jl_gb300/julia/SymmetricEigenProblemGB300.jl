@@ -16,6 +16,9 @@ and three additions without a reference counterpart:
     tridiag_eigen(d, e) -> (lam, Q), differentiable through a ChainRulesCore rrule whose
         pullback is the library's adjoint (FP64 tensor-core GEMMs with fused epilogues)
     bulk_wave_order_2x2_lmul!(A, givens)                      # bulk form of lmul!, src/simple_givens.jl:38
+    get_rotation(f, g) -> (c, s, r), elementwise               # src/simple_givens.jl:20
+    syev!(A) -> (lam, V): dense symmetric eigensolve (sytrd, orgtr, qr_algorithm!)
+    set_apply_form!(form), set_chase_mode!(mode): the library's arithmetic options
 
 Q may be Matrix{Float64} or Matrix{Float32} (the FP32-Q variant: FP64 chase, (c,s) rounded to
 Float32).  Host arrays are copied to the GPU and back by the library.  Nothing is exported,
@@ -23,6 +26,7 @@ as in the reference.  Unlike the reference, odd n is accepted.
 """
 module SymmetricEigenProblemGB300
 
+import LinearAlgebra
 using LinearAlgebra: SymTridiagonal, Diagonal, I
 using ChainRulesCore: ChainRulesCore, NoTangent, AbstractZero, unthunk
 
@@ -148,6 +152,43 @@ function ChainRulesCore.rrule(::typeof(tridiag_eigen), d::AbstractVector{Float64
     end
     return (lam, Q), tridiag_eigen_pullback
 end
+
+"""Elementwise get_rotation (LinearAlgebra.givensAlgorithm) computed on the device."""
+function get_rotation(f::Vector{Float64}, g::Vector{Float64})
+    length(f) == length(g) || throw(DimensionMismatch("f and g must have one length"))
+    c, s, r = similar(f), similar(f), similar(f)
+    st = ccall((:symeig_get_rotation_f64, libsymeig), Cint,
+        (Ptr{Cvoid}, Int64, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}),
+        handle(), length(f), f, g, c, s, r)
+    check(:symeig_get_rotation_f64, st)
+    return c, s, r
+end
+
+"""Dense symmetric eigensolve: (lam, V) with lam unsorted (as H.dv) and V the eigenvectors.
+A is left unchanged (the library copies it to the device)."""
+function syev!(A::StridedMatrix{Float64})
+    n = LinearAlgebra.checksquare(A)
+    stride(A, 1) == 1 || throw(ArgumentError("A must have unit row stride"))
+    lam = Vector{Float64}(undef, n)
+    V = Matrix{Float64}(undef, n, n)
+    conv = Ref{Int32}(0)
+    iter = Ref{Int64}(0)
+    st = GC.@preserve A ccall((:symeig_syev_f64, libsymeig), Cint,
+        (Ptr{Cvoid}, Int64, Ptr{Float64}, Int64, Ptr{Float64}, Ptr{Float64}, Int64, Ref{Int32}, Ref{Int64}),
+        handle(), n, A, stride(A, 2), lam, V, n, conv, iter)
+    check(:symeig_syev_f64, st)
+    conv[] != 0 || @warn "qr_algorithm! did not converge" iter[]
+    return lam, V
+end
+
+"""0: canonical rotations (default); 1: the scaled form of the FP64 bulk apply."""
+set_apply_form!(form::Integer) =
+    check(:symeig_set_apply_form, ccall((:symeig_set_apply_form, libsymeig), Cint, (Ptr{Cvoid}, Int32), handle(), form))
+
+"""0: Newton-form two-warp chase (default); 1: reference form; 2: Newton form with every
+sweep redone in the reference form.  All give the same bits."""
+set_chase_mode!(mode::Integer) =
+    check(:symeig_set_chase_mode, ccall((:symeig_set_chase_mode, libsymeig), Cint, (Ptr{Cvoid}, Int32), handle(), mode))
 
 function eigen_decomp!(H::SymTridiagonal{Float64})
     n = size(H, 1)
