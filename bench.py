@@ -669,6 +669,7 @@ def run_adjoint(args):
     e1.record()
     torch.cuda.synchronize()
     adj_ms = e0.elapsed_time(e1)
+    dmma_peak = pkg._lib.measure_dmma_peak(0)
     # batched variant: 256 matrices of n = 512
     B, nb = 256, 512
     db = torch.tensor(rng.standard_normal((B, nb)), device=dev, requires_grad=True)
@@ -702,6 +703,10 @@ def run_adjoint(args):
         "grad_rel_err_vs_fp64_reference": rel,
         "adjoint_kernels_ms": round(adj_ms, 2),
         "adjoint_gemm_tflops": round(4.0 * n ** 3 / (adj_ms * 1e-3) / 1e12, 3),
+        "roofline": {"bound": "fp64 tensor (mma.sync .f64)", "achieved": round(4.0 * n ** 3 / (adj_ms * 1e-3) / 1e12, 3),
+                     "peak": round(dmma_peak, 3), "unit": "TFLOP/s",
+                     "frac": round(4.0 * n ** 3 / (adj_ms * 1e-3) / 1e12 / dmma_peak, 4),
+                     "peak_source": "measured now by symeig_measure_dmma_peak"},
         "batched": {"B": B, "n": nb, "forward_s": round(t1 - t0, 3), "backward_s": round(t2 - t1, 3),
                     "ratio": round((t2 - t0) / (t1 - t0), 4)},
         "clocks": clk.summary(),
@@ -759,6 +764,7 @@ def run_dense(args):
         "config": {"workload": "syev: sytrd -> orgtr -> qr_algorithm!", "n": n},
         "sytrd_s": round(t1 - t0, 3), "orgtr_s": round(t2 - t1, 3), "qr_s": round(t3 - t2, 3),
         "sytrd_gflops": round(flops / (t1 - t0) / 1e9, 1), "orgtr_gflops": round(flops / (t2 - t1) / 1e9, 1),
+        "dmma_peak_tflops": round(pkg._lib.measure_dmma_peak(0), 3),
         "converged": bool(conv), "iterations": it,
         "errors": {"eig_max_abs_vs_lapack": eig_err, "eig_bound_10n_eps_normA": 10 * n * eps * float(np.max(np.abs(ref))),
                    "resid_rel": resid, "orth": orth, "bound_10n_eps": 10 * n * eps},

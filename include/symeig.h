@@ -95,6 +95,9 @@ int symeig_set_kernel_timing(symeig_handle h, int32_t on);
  * else FP32: the roofline denominator of the Givens kernels.  Runs ~10 ms.  No reference
  * counterpart (the README compares with LinearAlgebra.peakflops(), README.md:28-31). */
 int symeig_measure_fma_peak(int device, int32_t fp64, double* tflops);
+/* The FP64 tensor-core (mma.sync .f64) rate, TFLOP/s, measured the same way: the roofline
+ * denominator of the adjoint and dense-reduction GEMMs.  No reference counterpart. */
+int symeig_measure_dmma_peak(int device, double* tflops);
 const char* symeig_status_string(int status);
 /* Device properties the library tuned for (SM count, FP64/FP32 launch shapes). */
 int symeig_device_info(symeig_handle h, int32_t* sm_count, int32_t* cc_major, int32_t* cc_minor);

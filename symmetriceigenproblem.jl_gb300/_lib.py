@@ -44,6 +44,7 @@ SIGNATURES = {
     "symeig_get_rotation_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "symeig_set_kernel_timing": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, c_i32, ctypes.POINTER(c_dbl)]),
+    "symeig_measure_dmma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(c_dbl)]),
     "symeig_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "symeig_device_info": (ctypes.c_int, [c_vp, P_i32, P_i32, P_i32]),
     "symeig_qr_f64": (ctypes.c_int, [c_vp, c_vp, c_vp, c_i64, c_vp, c_i64, c_i64, c_i32, c_dbl, c_i64, P_i32, P_i64]),
@@ -195,6 +196,13 @@ def measure_fma_peak(device: int = 0, fp64: bool = True) -> float:
     """FMA throughput of the device now, TFLOP/s (FMA = 2 flops)."""
     v = c_dbl()
     check("symeig_measure_fma_peak", load().symeig_measure_fma_peak(device, int(fp64), ctypes.byref(v)))
+    return v.value
+
+
+def measure_dmma_peak(device: int = 0) -> float:
+    """FP64 tensor-core (mma.sync .f64) throughput of the device now, TFLOP/s."""
+    v = c_dbl()
+    check("symeig_measure_dmma_peak", load().symeig_measure_dmma_peak(device, ctypes.byref(v)))
     return v.value
 
 
