@@ -87,6 +87,12 @@ int symeig_set_chase_mode(symeig_handle h, int32_t mode);
  * of the same form bit for bit.  The FP32, left, batched and allocation-free applies always
  * use form 0.  No reference counterpart. */
 int symeig_set_apply_form(symeig_handle h, int32_t form);
+/* Test hook for the failure path of the bounded device waits: with chunk > 0 the wave
+ * kernels stop copying their rotation table from that chunk on, so their waits run out
+ * (~2 s of SM clock), the kernels return without touching Q further, and the synchronous
+ * entry points return SYMEIG_ERR_TIMEOUT (device_errors = 1 in the statistics).  Q is then
+ * unspecified; the handle and the context stay usable.  0 (default) turns it off. */
+int symeig_set_test_stall(symeig_handle h, int32_t chunk);
 /* Record CUDA events around every wave-kernel launch so symeig_get_stats can report their
  * device time (wave_kernel_ms).  Off by default.  symeig_get_stats waits for the last
  * marked launch.  No reference counterpart (the reference times with BenchmarkTools). */

@@ -34,6 +34,7 @@ SIGNATURES = {
     "symeig_set_exact_order": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_chase_mode": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_apply_form": (ctypes.c_int, [c_vp, c_i32]),
+    "symeig_set_test_stall": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_get_rotation_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "symeig_sytrd_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp]),
     "symeig_sytrd_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_vp]),

@@ -60,6 +60,7 @@ struct symeig_context {
     int32_t exact_order = 1;  // rotation placement of the qr driver
     int32_t chase_mode = 0;   // symeig_set_chase_mode
     int32_t apply_form = 0;   // symeig_set_apply_form
+    int32_t test_stall = 0;   // symeig_set_test_stall
     ChaseState* h_state = nullptr;  // pinned
     std::vector<cudaEvent_t> timing;  // pool of timing events
     symeig_stats stats{};
@@ -133,6 +134,17 @@ void begin_call(symeig_handle h)
     std::memset(&h->stats, 0, sizeof(h->stats));
     h->kused = 0;
     h->kpending = false;
+    // the error word of the bounded waits reports on this call only
+    cudaMemsetAsync(h->derr, 0, sizeof(int), h->stream);
+}
+
+// After a synchronous call: SYMEIG_ERR_TIMEOUT if a wave kernel's bounded wait gave up.
+int check_device_error(symeig_handle h)
+{
+    int derr = 0;
+    CK(cudaMemcpy(&derr, h->derr, sizeof(int), cudaMemcpyDeviceToHost));
+    h->stats.device_errors = derr;
+    return derr ? SYMEIG_ERR_TIMEOUT : SYMEIG_OK;
 }
 
 // Run every pass of one bulk apply of `layers` layers of `grid` to columns [c0, c0+n_loc).
@@ -147,6 +159,7 @@ int apply_grid(symeig_handle h, T* Q, int64_t ldq, int64_t m, const Tsrc* grid, 
     for (int64_t L0 = 0; L0 < layers; L0 += per) {
         ApplyPass pass{c0, n_loc, L0, std::min(per, layers - L0), rs};
         pass.form = sizeof(T) == 8 ? h->apply_form : 0;
+        pass.stall = h->test_stall;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (h->kernel_timing) {
             e0 = kernel_event(h);
@@ -289,6 +302,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     h->stats.apply_ms = apply_ms;
     h->stats.total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    if (result == SYMEIG_OK) result = check_device_error(h);
     return result;
 }
 
@@ -372,7 +386,7 @@ int apply_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T
     CK(cudaStreamSynchronize(s));
     h->stats.total_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    return SYMEIG_OK;
+    return check_device_error(h);
 }
 
 // Row rotations (lmul!, src/simple_givens.jl:38-51) of an m x n column-major A: the wave
@@ -579,6 +593,14 @@ int symeig_set_apply_form(symeig_handle h, int32_t form)
     if (!h) return SYMEIG_ERR_HANDLE;
     if (form < 0 || form > 1) return SYMEIG_ERR_SIZE;
     h->apply_form = form;
+    return SYMEIG_OK;
+}
+
+int symeig_set_test_stall(symeig_handle h, int32_t chunk)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    if (chunk < 0) return SYMEIG_ERR_SIZE;
+    h->test_stall = chunk;
     return SYMEIG_OK;
 }
 

@@ -244,7 +244,7 @@ template <typename T, int S, bool SCALED = false>
 __global__ void __launch_bounds__(kThreads, Cfg<T, S>::MINB)
 wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
                   const unsigned char* __restrict__ table, int32_t n_chunks, int* __restrict__ err,
-                  const T nz, int64_t rs)
+                  const T nz, int64_t rs, int32_t stall)
 {
     using Sh = typename Cfg<T, S>::Sh;
     __shared__ __align__(128) unsigned char ring[2][Sh::CHUNK];
@@ -252,7 +252,7 @@ wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
     wave::Staging<Sh> st{ring, bar, 0, 0};
     wave::staging_init(st);
     const int64_t row0 = (int64_t)blockIdx.x * Sh::ROWS;
-    if (!wave::wave_tile<T, Sh, SCALED>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs)) {
+    if (!wave::wave_tile<T, Sh, SCALED>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs, stall)) {
         if (threadIdx.x == 0) atomicExch(err, 1);
     }
 }
@@ -324,7 +324,7 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
             if (ev_begin) cudaEventRecord(ev_begin, stream);
             wave_apply_kernel<T, S, true><<<(unsigned)blocks, kThreads, 0, stream>>>(
                 Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
-                (int32_t)n_chunks, err, (T)-0.0, pass.rs);
+                (int32_t)n_chunks, err, (T)-0.0, pass.rs, pass.stall > 0 ? pass.stall : 0x7fffffff);
             e = cudaGetLastError();
             if (ev_end) cudaEventRecord(ev_end, stream);
             return e;
@@ -341,7 +341,7 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
     if (ev_begin) cudaEventRecord(ev_begin, stream);
     wave_apply_kernel<T, S><<<(unsigned)blocks, kThreads, 0, stream>>>(
         Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
-        (int32_t)n_chunks, err, (T)-0.0, pass.rs);
+        (int32_t)n_chunks, err, (T)-0.0, pass.rs, pass.stall > 0 ? pass.stall : 0x7fffffff);
     e = cudaGetLastError();
     if (ev_end) cudaEventRecord(ev_end, stream);
     return e;

@@ -86,6 +86,7 @@ struct ApplyPass {
     int64_t c0, n_loc, L0, layers;
     int64_t rs = 1;  // stride between the kernel's rows (1: rmul!, lda: lmul! on the transpose)
     int32_t form = 0;  // 0 canonical rotations, 1 the scaled form (FP64 only; see apply.cu)
+    int32_t stall = 0; // test hook: > 0 stops the table copies from that chunk on (see wave_tile)
 };
 
 // Layers one pass of the wave-window kernel handles for element type T.

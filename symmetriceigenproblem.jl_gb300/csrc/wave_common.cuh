@@ -213,7 +213,9 @@ __device__ __forceinline__ void staging_init(Staging<Sh>& st)
 }
 
 // One tile: rows [row0, row0 + ROWS) of Q (m rows, columns [0, n_loc) of the pass) through
-// the n_chunks chunks of `table`.  Element (row, col) is Q[row * rs + col * ldq]: rs = 1 for
+// the n_chunks chunks of `table`.  `stall` (a test hook, default never): chunks from that
+// index on are not copied, so their bounded waits run out and the tile returns false.
+// Element (row, col) is Q[row * rs + col * ldq]: rs = 1 for
 // the column rotations of rmul! on a column-major matrix, rs = lda and ldq = 1 for the row
 // rotations of lmul! (the same wave on the transposed view).  Every thread of the CTA calls
 // it.  Returns false (all threads) when a bounded wait gave up.
@@ -221,14 +223,14 @@ template <typename T, typename Sh, bool SCALED = false>
 __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_t m, int64_t row0,
                                           int32_t n_loc, const unsigned char* __restrict__ table,
                                           int32_t n_chunks, const T nz, Staging<Sh>& st,
-                                          int64_t rs = 1)
+                                          int64_t rs = 1, int32_t stall = 0x7fffffff)
 {
     constexpr int KB = Sh::KB, G = Sh::G, CH = Sh::CH, W = Sh::W, RPW = Sh::RPW;
     const int tid = threadIdx.x;
     if (tid == 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         bulk_load(st.ring[0], table, Sh::CHUNK, &st.bar[0]);
-        if (n_chunks > 1) bulk_load(st.ring[1], table + Sh::CHUNK, Sh::CHUNK, &st.bar[1]);
+        if (n_chunks > 1 && stall > 1) bulk_load(st.ring[1], table + Sh::CHUNK, Sh::CHUNK, &st.bar[1]);
     }
 
     const int lane = tid & 31;
@@ -303,7 +305,7 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
             }
         }
         __syncthreads();
-        if (tid == 0 && c + 2 < n_chunks) {
+        if (tid == 0 && c + 2 < n_chunks && c + 2 < stall) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             bulk_load(st.ring[b], table + (int64_t)(c + 2) * Sh::CHUNK, Sh::CHUNK, &st.bar[b]);
         }
