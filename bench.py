@@ -164,6 +164,24 @@ def cpu_wave_gflops(m, n, k, dtype, threads, target_s=8.0, max_rows=None):
         rows = int(min(cap, rows * max(2.0, min(16.0, target_s / max(dt, 1e-3)))))
 
 
+def replica_reduce(ms: float, world: int, device=None) -> float:
+    """The job time of N independent replicas: the slowest rank's (all_reduce MAX); every
+    rank returns it.  With world == 1 it is the rank's own time."""
+    if world <= 1:
+        return ms
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(work_per_rank: float, world: int, ms: float) -> float:
+    """Whole-job throughput: the work of all replicas over the slowest replica's time (the
+    path does not shard, so every rank does the same work on its own GPU)."""
+    return work_per_rank * world / (ms * 1e-3)
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -258,15 +276,12 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
     clocks = clk.summary()
-    ms = e0.elapsed_time(e1)
+    ms = replica_reduce(e0.elapsed_time(e1), world, dev)
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
         dist.barrier()
     ms_per_step = ms / args.steps
     fl = flops_per_step(m, n, k)
-    value = fl * world / (ms_per_step * 1e-3) / 1e9
+    value = replica_value(fl, world, ms_per_step) / 1e9
 
     # roofline of the dominant kernel: the FP64 (FP32) FMA pipe
     peak = pkg._lib.measure_fma_peak(local, fp64=(args.dtype == "f64"))
@@ -295,11 +310,7 @@ def run_ours(args):
     e2e_steps = max(1, min(args.steps, 3))
     for _ in range(e2e_steps):
         e2e_step()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = replica_reduce((time.perf_counter() - t0) / e2e_steps * 1e3, world, dev) * 1e-3
     esz = 8 if args.dtype == "f64" else 4
     e2e = {"value": round(fl * world / e2e_s / 1e9, 3), "unit": "GFLOP/s",
            "h2d_bytes_per_step": int(m * n * esz + (n - 1) * k * 2 * esz),
