@@ -212,6 +212,22 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def hbm_side(algo_bytes: float, flops_per_launch: float, kernel_ms: float, peak_tflops: float) -> dict:
+    """The other side of the roofline min(FMA peak, HBM bandwidth x intensity), with the HBM
+    copy bandwidth measured on this machine (MEASURED_PEAKS.json)."""
+    try:
+        bw = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"])
+        src = "MEASURED_PEAKS.json"
+    except Exception:
+        bw, src = 6800.0, "fallback 6.8 TB/s"
+    intensity = flops_per_launch / algo_bytes
+    achieved = algo_bytes / (kernel_ms * 1e-3) / 1e9
+    return {"bandwidth_gbs": bw, "bandwidth_source": src, "intensity_flop_per_byte": round(intensity, 2),
+            "bw_x_intensity_tflops": round(bw * intensity / 1e3, 1),
+            "roofline_tflops": round(min(peak_tflops, bw * intensity / 1e3), 4),
+            "achieved_gbs": round(achieved, 1), "frac_of_bandwidth": round(achieved / bw, 4)}
+
+
 def read_traffic():
     """DRAM bytes per launch of the wave kernel from the committed ncu summary, if present."""
     try:
@@ -349,6 +365,7 @@ def run_ours(args):
                                         "a Givens rotation-row is 4 FMA-pipe ops for 6 counted flops, so 0.75 is the ceiling"
                                         + ("; the scaled form spends 2 FMAs per rotation-row, so its ceiling is 1.5 and "
                                            "fp64_pipe_frac is the measure of pipe use" if form else ""),
+                         "hbm": hbm_side(algo_bytes, fl / passes, per_launch_ms, peak),
                          "fp64_instr_per_rotation_row": 2 if form else 4,
                          "fp64_pipe_frac": round((2 if form else 4) * (fl / 6.0 / passes) / (per_launch_ms * 1e-3)
                                                  / (peak * 1e12 / 2.0), 4),
