@@ -49,7 +49,7 @@ struct Shape {
     static constexpr int KB = KB_, G = G_, W = KB_ + 1;
     static constexpr int RPW = 32 / G;                          // rows per warp
     static constexpr int ROWS = RPW * (kThreads / 32);          // rows per tile
-    static constexpr int CH = (sizeof(T) == 8 ? 1 : 2) * W;     // iterations per chunk
+    static constexpr int CH = W;                                // iterations per chunk
     static constexpr int GSTRIDE = KB * (int)sizeof(P2) + 16;   // bytes per group, padded
     static constexpr int ITER = G * GSTRIDE;                    // bytes per iteration
     static constexpr int CHUNK = CH * ITER;                     // bytes per chunk
