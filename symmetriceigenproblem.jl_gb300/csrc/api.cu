@@ -777,7 +777,7 @@ int symeig_apply_tuning(int32_t fp64, int32_t* shape, int32_t set)
 {
     if (!shape) return SYMEIG_ERR_NULL;
     if (set) {
-        if (*shape < 0 || *shape > 1) return SYMEIG_ERR_SIZE;
+        if (*shape < 0 || *shape >= apply_num_shapes(fp64)) return SYMEIG_ERR_SIZE;
         apply_set_shape(fp64, *shape);
     } else {
         *shape = apply_get_shape(fp64);

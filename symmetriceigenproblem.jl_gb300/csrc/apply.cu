@@ -24,16 +24,26 @@ using wave::kThreads;
 //             SM sub-partition.  The FP64 choice: the FP64 unit (2 FMA per SM per clock on
 //             GB300) is the limit and this shape balances it best.
 //   shape 1 = 4 lane groups of 16 layers: 8 rows per warp, twice the rotations per wave for
-//             the same per-wave overhead (shuffle, Q load/store, address arithmetic).  The
-//             FP32 choice: FP32 is issue-bound, so overhead per rotation matters more than
-//             the coarser balance.
+//             the same per-wave overhead (shuffle, Q load/store, address arithmetic).  For
+//             FP32 the overhead per rotation matters more than the coarser balance.
+//   shapes 2, 3 (FP32 only) = shapes 1, 0 with 2 rows per thread: each (c,s) pair read from
+//             shared memory serves two rows, so the shared-memory pipe (2 wavefronts per
+//             128-bit broadcast read of 4 or 8 distinct addresses) carries half the load per
+//             rotation-row, and each thread has two independent rotation chains.  Shape 2
+//             is the FP32 choice (1.5-3 % ahead of shape 1, measured).
 template <typename T, int S> struct Cfg;
 template <> struct Cfg<double, 0> { using Sh = Shape<double, 8, 8>; static constexpr int MINB = 7; };
 template <> struct Cfg<double, 1> { using Sh = Shape<double, 16, 4>; static constexpr int MINB = 4; };
 template <> struct Cfg<float, 0> { using Sh = Shape<float, 8, 8>; static constexpr int MINB = 7; };
 template <> struct Cfg<float, 1> { using Sh = Shape<float, 16, 4>; static constexpr int MINB = 5; };
+template <> struct Cfg<float, 2> { using Sh = Shape<float, 16, 4, 2>; static constexpr int MINB = 3; };
+template <> struct Cfg<float, 3> { using Sh = Shape<float, 8, 8, 2>; static constexpr int MINB = 4; };
+// the table depends on (KB, G) only, so shapes 2 and 3 share the tables of 1 and 0
+static_assert(Cfg<float, 2>::Sh::CHUNK == Cfg<float, 1>::Sh::CHUNK, "table layout");
+static_assert(Cfg<float, 3>::Sh::CHUNK == Cfg<float, 0>::Sh::CHUNK, "table layout");
 
-int g_shape[2] = {0, 1};  // [0] FP64, [1] FP32
+constexpr int kShapes[2] = {2, 4};  // shapes available to [0] FP64, [1] FP32
+int g_shape[2] = {0, 2};            // [0] FP64, [1] FP32
 template <typename T> int shape_index() { return g_shape[sizeof(T) == 8 ? 0 : 1]; }
 
 template <typename Tsrc, typename T, int S>
@@ -352,14 +362,27 @@ cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t g
                        const int32_t* place, const ApplyPass& pass, void* table, int* err,
                        cudaStream_t stream, cudaEvent_t ev_begin, cudaEvent_t ev_end)
 {
-    if (shape_index<T>() == 0)
+    const int s = shape_index<T>();
+    if constexpr (sizeof(T) == 4) {
+        if (s == 2)
+            return apply_pass_shape<Tsrc, T, 2>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
+                                                stream, ev_begin, ev_end);
+        if (s == 3)
+            return apply_pass_shape<Tsrc, T, 3>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
+                                                stream, ev_begin, ev_end);
+    }
+    if (s == 0)
         return apply_pass_shape<Tsrc, T, 0>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
                                             stream, ev_begin, ev_end);
     return apply_pass_shape<Tsrc, T, 1>(Q, ldq, m, grid, grid_rows, place, pass, table, err, stream,
                                         ev_begin, ev_end);
 }
 
-void apply_set_shape(int fp64, int shape) { g_shape[fp64 ? 0 : 1] = shape ? 1 : 0; }
+int apply_num_shapes(int fp64) { return kShapes[fp64 ? 0 : 1]; }
+void apply_set_shape(int fp64, int shape)
+{
+    g_shape[fp64 ? 0 : 1] = (shape >= 0 && shape < apply_num_shapes(fp64)) ? shape : 0;
+}
 int apply_get_shape(int fp64) { return g_shape[fp64 ? 0 : 1]; }
 
 template cudaError_t apply_pass<double, double>(double*, int64_t, int64_t, const double*, int64_t,

@@ -114,6 +114,7 @@ cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t g
 // Tile shape of the single-matrix wave kernel per precision (see apply.cu).
 void apply_set_shape(int fp64, int shape);
 int apply_get_shape(int fp64);
+int apply_num_shapes(int fp64);  // tile shapes available to FP64 (fp64 != 0) or FP32
 
 // Dense symmetric -> tridiagonal (sytrd.cu).  Scratch sizes in doubles.
 int64_t dense_scratch_doubles(int64_t n);

@@ -1,8 +1,8 @@
 // wave_common.cuh -- the wave-window Givens tile shared by the single-matrix and the batched
 // apply kernels.
 //
-// A tile is the work of one CTA of 4 warps: 4 * (32/G) consecutive rows of Q, all columns of
-// the pass, all G*KB layers of the pass.
+// A tile is the work of one CTA of 4 warps: 4 * R * (32/G) consecutive rows of Q (R rows per
+// thread), all columns of the pass, all G*KB layers of the pass.
 //
 // Order of the rotations.  Rotation (i, L) acts on columns (i, i+1).  The reference's wave
 // order (src/wave.jl:62-162) applies (i, L) after (i-1, L) and after (i+1, L-1); per element
@@ -11,8 +11,8 @@
 // (t-1-l, l) for l = 0..KB-1, i.e. the column pairs (t-1-l, t-l) from right to left, which
 // respects both dependencies.  After wave t, column t-KB is final for the group.
 //
-// Layer groups.  The G groups of a row run in the G lane groups of one warp (32/G rows per
-// warp).  Group g lags group g-1 by KB+1 waves and receives its input columns from group g-1
+// Layer groups.  The G groups of a row run in the G lane groups of one warp (R * 32/G rows
+// per warp).  Group g lags group g-1 by KB+1 waves and receives its input columns from group g-1
 // through a warp shuffle, so a pass reads and writes each element of Q once.  All groups of a
 // warp hold the same rows, so the column read issued by every lane costs one sector per
 // warp; group 0 keeps it, group G-1 stores the finished column.
@@ -43,12 +43,13 @@ namespace wave {
 
 constexpr int kThreads = 128;  // 4 warps per CTA
 
-template <typename T, int KB_, int G_>
+template <typename T, int KB_, int G_, int R_ = 1>
 struct Shape {
     using P2 = typename Pair<T>::type;
     static constexpr int KB = KB_, G = G_, W = KB_ + 1;
-    static constexpr int RPW = 32 / G;                          // rows per warp
-    static constexpr int ROWS = RPW * (kThreads / 32);          // rows per tile
+    static constexpr int R = R_;                                // rows per thread
+    static constexpr int RPW = 32 / G;                          // lanes per group
+    static constexpr int ROWS = R * RPW * (kThreads / 32);      // rows per tile
     static constexpr int CH = W;                                // iterations per chunk
     static constexpr int GSTRIDE = KB * (int)sizeof(P2) + 16;   // bytes per group, padded
     static constexpr int ITER = G * GSTRIDE;                    // bytes per iteration
@@ -143,11 +144,12 @@ __device__ __forceinline__ void table_entry(unsigned char* table, int64_t t, int
     *(P2*)(table + t * Sh::ITER + g * Sh::GSTRIDE + l * (int)sizeof(P2)) = v;
 }
 
-// The KB rotations of one wave on the window, (c,s) read from shared memory.  U is the wave's
-// slot (t mod (KB+1)); callers pass a constant of a fully unrolled loop, so every window
-// index folds to a constant and the window stays in registers.
-template <typename T, int KB>
-__device__ __forceinline__ void wave_rotations(T (&win)[KB + 1], const unsigned char* cs, const int U,
+// The KB rotations of one wave on the windows of the thread's R rows, (c,s) read from shared
+// memory once for all R rows.  U is the wave's slot (t mod (KB+1)); callers pass a constant of
+// a fully unrolled loop, so every window index folds to a constant and the windows stay in
+// registers.
+template <typename T, int KB, int R>
+__device__ __forceinline__ void wave_rotations(T (&win)[R][KB + 1], const unsigned char* cs, const int U,
                                                const T nz)
 {
     constexpr int W = KB + 1;
@@ -155,14 +157,19 @@ __device__ __forceinline__ void wave_rotations(T (&win)[KB + 1], const unsigned 
 #pragma unroll
         for (int l = 0; l < KB; ++l) {
             const double2 p = *reinterpret_cast<const double2*>(cs + l * 16);
-            rot_fma(win[(U - 1 - l + 2 * W) % W], win[(U - l + 2 * W) % W], p.x, p.y, nz);
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                rot_fma(win[r][(U - 1 - l + 2 * W) % W], win[r][(U - l + 2 * W) % W], p.x, p.y, nz);
         }
     } else {
 #pragma unroll
         for (int l = 0; l < KB; l += 2) {
             const float4 p = *reinterpret_cast<const float4*>(cs + l * 8);
-            rot(win[(U - 1 - l + 2 * W) % W], win[(U - l + 2 * W) % W], p.x, p.y);
-            rot(win[(U - 2 - l + 2 * W) % W], win[(U - 1 - l + 2 * W) % W], p.z, p.w);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                rot(win[r][(U - 1 - l + 2 * W) % W], win[r][(U - l + 2 * W) % W], p.x, p.y);
+                rot(win[r][(U - 2 - l + 2 * W) % W], win[r][(U - 1 - l + 2 * W) % W], p.z, p.w);
+            }
         }
     }
 }
@@ -172,8 +179,8 @@ __device__ __forceinline__ void wave_rotations(T (&win)[KB + 1], const unsigned 
 // l set) or form 1.  With (u, v) = form 2 ? (y, x) : (x, y):  x = fma(A, v, u), y = fma(B, u, v)
 // -- two FP64 instructions per rotation-row instead of four.  The scale factors the form
 // folds out of the columns are applied once per pass when group G-1 stores a column.
-template <int KB>
-__device__ __forceinline__ void wave_rotations_scaled(double (&win)[KB + 1], const unsigned char* cs,
+template <int KB, int R>
+__device__ __forceinline__ void wave_rotations_scaled(double (&win)[R][KB + 1], const unsigned char* cs,
                                                       const int U)
 {
     constexpr int W = KB + 1;
@@ -181,12 +188,15 @@ __device__ __forceinline__ void wave_rotations_scaled(double (&win)[KB + 1], con
 #pragma unroll
     for (int l = 0; l < KB; ++l) {
         const double2 p = *reinterpret_cast<const double2*>(cs + l * 16);
-        double& x = win[(U - 1 - l + 2 * W) % W];
-        double& y = win[(U - l + 2 * W) % W];
         const bool f2 = (flags >> l) & 1u;
-        const double u = f2 ? y : x, v = f2 ? x : y;
-        x = __fma_rn(p.x, v, u);
-        y = __fma_rn(p.y, u, v);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            double& x = win[r][(U - 1 - l + 2 * W) % W];
+            double& y = win[r][(U - l + 2 * W) % W];
+            const double u = f2 ? y : x, v = f2 ? x : y;
+            x = __fma_rn(p.x, v, u);
+            y = __fma_rn(p.y, u, v);
+        }
     }
 }
 
@@ -225,7 +235,7 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
                                           int32_t n_chunks, const T nz, Staging<Sh>& st,
                                           int64_t rs = 1, int32_t stall = 0x7fffffff)
 {
-    constexpr int KB = Sh::KB, G = Sh::G, CH = Sh::CH, W = Sh::W, RPW = Sh::RPW;
+    constexpr int KB = Sh::KB, G = Sh::G, CH = Sh::CH, W = Sh::W, RPW = Sh::RPW, R = Sh::R;
     const int tid = threadIdx.x;
     if (tid == 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -233,22 +243,34 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
         if (n_chunks > 1 && stall > 1) bulk_load(st.ring[1], table + Sh::CHUNK, Sh::CHUNK, &st.bar[1]);
     }
 
+    // lane rl of group g holds rows rbase + r*RPW, r < R, of the warp's R*RPW rows
     const int lane = tid & 31;
     const int g = lane / RPW;
     const int rl = lane - g * RPW;
-    const int64_t row = row0 + (tid >> 5) * RPW + rl;
-    const bool row_ok = row < m;
-    T* __restrict__ qrow = Q + (row_ok ? row : 0) * rs;
-    const bool storer = (g == G - 1) && row_ok;  // group G-1 writes Q
-    const int lag = g * W;                       // waves this group trails group 0
-
-    T win[W], ahead[W];
+    const int64_t rbase = row0 + (int64_t)(tid >> 5) * (R * RPW) + rl;
+    T* __restrict__ qrow[R];
+    bool storer[R];  // group G-1 writes Q
 #pragma unroll
-    for (int q = 0; q < W; ++q) {
-        win[q] = T(0);
-        ahead[q] = (q < n_loc) ? qrow[(int64_t)q * ldq] : T(0);
+    for (int r = 0; r < R; ++r) {
+        const int64_t row = rbase + (int64_t)r * RPW;
+        const bool row_ok = row < m;
+        qrow[r] = Q + (row_ok ? row : 0) * rs;
+        storer[r] = (g == G - 1) && row_ok;
     }
-    T xout = T(0);
+    const int lag = g * W;  // waves this group trails group 0
+
+    T win[R][W], ahead[R][W];
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+#pragma unroll
+        for (int q = 0; q < W; ++q) {
+            win[r][q] = T(0);
+            ahead[r][q] = (q < n_loc) ? qrow[r][(int64_t)q * ldq] : T(0);
+        }
+    }
+    T xout[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) xout[r] = T(0);
 
     for (int32_t c = 0; c < n_chunks; ++c) {
         const int b = c & 1;
@@ -259,30 +281,40 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
         const int32_t t0 = c * CH;
         // column t0 + u + W is read in iteration u; group G-1 writes column t0 + u - lag - KB
         const int32_t st0 = t0 - lag - KB;
-        const T* ld_base = qrow + (int64_t)(t0 + W) * ldq;
-        T* st_base = qrow + (int64_t)st0 * ldq;
         const bool interior = (t0 + W + CH <= n_loc) && (t0 - (G - 1) * W - KB >= 0) &&
                               (t0 - KB + CH <= n_loc);
         if (interior) {
-            const T* lp = ld_base;
-            T* sp = st_base;
+            const T* lp[R];
+            T* sp[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                lp[r] = qrow[r] + (int64_t)(t0 + W) * ldq;
+                sp[r] = qrow[r] + (int64_t)st0 * ldq;
+            }
 #pragma unroll
             for (int u = 0; u < CH; ++u) {
-                const T up = __shfl_up_sync(0xffffffffu, xout, RPW);
-                const T xin = (g == 0) ? ahead[u % W] : up;
-                ahead[u % W] = *lp;
-                lp += ldq;
-                win[u % W] = xin;
-                if constexpr (SCALED) wave_rotations_scaled<KB>(win, sb + u * Sh::ITER, u % W);
-                else wave_rotations<T, KB>(win, sb + u * Sh::ITER, u % W, nz);
-                xout = win[(u + 1) % W];
-                if constexpr (SCALED) {
-                    const T dsc = *reinterpret_cast<const T*>(sb + u * Sh::ITER + KB * 16 + 8);
-                    if (storer) *sp = xout * dsc;
-                } else {
-                    if (storer) *sp = xout;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const T up = __shfl_up_sync(0xffffffffu, xout[r], RPW);
+                    const T xin = (g == 0) ? ahead[r][u % W] : up;
+                    ahead[r][u % W] = *lp[r];
+                    lp[r] += ldq;
+                    win[r][u % W] = xin;
                 }
-                sp += ldq;
+                if constexpr (SCALED) wave_rotations_scaled<KB, R>(win, sb + u * Sh::ITER, u % W);
+                else wave_rotations<T, KB, R>(win, sb + u * Sh::ITER, u % W, nz);
+                T dsc = T(1);
+                if constexpr (SCALED) dsc = *reinterpret_cast<const T*>(sb + u * Sh::ITER + KB * 16 + 8);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    xout[r] = win[r][(u + 1) % W];
+                    if constexpr (SCALED) {
+                        if (storer[r]) *sp[r] = xout[r] * dsc;
+                    } else {
+                        if (storer[r]) *sp[r] = xout[r];
+                    }
+                    sp[r] += ldq;
+                }
             }
         } else {
             const int32_t ld_cnt = min(max(n_loc - t0 - W, 0), CH);
@@ -290,18 +322,26 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
             const int32_t st_hi = min(n_loc - st0, CH);
 #pragma unroll
             for (int u = 0; u < CH; ++u) {
-                const T up = __shfl_up_sync(0xffffffffu, xout, RPW);
-                const T xin = (g == 0) ? ahead[u % W] : up;
-                T nxt = T(0);
-                if (u < ld_cnt) nxt = ld_base[(int64_t)u * ldq];
-                ahead[u % W] = nxt;
-                win[u % W] = xin;
-                if constexpr (SCALED) wave_rotations_scaled<KB>(win, sb + u * Sh::ITER, u % W);
-                else wave_rotations<T, KB>(win, sb + u * Sh::ITER, u % W, nz);
-                xout = win[(u + 1) % W];
-                T xs = xout;
-                if constexpr (SCALED) xs = xout * *reinterpret_cast<const T*>(sb + u * Sh::ITER + KB * 16 + 8);
-                st_pred(st_base + (int64_t)u * ldq, xs, storer && u >= st_lo && u < st_hi);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const T up = __shfl_up_sync(0xffffffffu, xout[r], RPW);
+                    const T xin = (g == 0) ? ahead[r][u % W] : up;
+                    T nxt = T(0);
+                    if (u < ld_cnt) nxt = qrow[r][(int64_t)(t0 + W + u) * ldq];
+                    ahead[r][u % W] = nxt;
+                    win[r][u % W] = xin;
+                }
+                if constexpr (SCALED) wave_rotations_scaled<KB, R>(win, sb + u * Sh::ITER, u % W);
+                else wave_rotations<T, KB, R>(win, sb + u * Sh::ITER, u % W, nz);
+                T dsc = T(1);
+                if constexpr (SCALED) dsc = *reinterpret_cast<const T*>(sb + u * Sh::ITER + KB * 16 + 8);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    xout[r] = win[r][(u + 1) % W];
+                    T xs = xout[r];
+                    if constexpr (SCALED) xs = xout[r] * dsc;
+                    st_pred(qrow[r] + (int64_t)(st0 + u) * ldq, xs, storer[r] && u >= st_lo && u < st_hi);
+                }
             }
         }
         __syncthreads();

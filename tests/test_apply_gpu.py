@@ -63,10 +63,11 @@ def test_left_apply_matches_oracle(cuda, pkg, oracle, m, n, k, dtype):
     assert np.array_equal(B, refT.T)
 
 
-@pytest.mark.parametrize("dtype", [np.float64, np.float32])
-@pytest.mark.parametrize("shape", [0, 1])
-def test_apply_both_tile_shapes(cuda, pkg, oracle, dtype, shape):
-    """Both tile shapes of the single-matrix wave kernel give the oracle's bits."""
+@pytest.mark.parametrize("dtype,shape", [(np.float64, 0), (np.float64, 1), (np.float32, 0),
+                                         (np.float32, 1), (np.float32, 2), (np.float32, 3)])
+def test_apply_every_tile_shape(cuda, pkg, oracle, dtype, shape):
+    """Every tile shape of the single-matrix wave kernel gives the oracle's bits (FP32 shapes 2
+    and 3 hold two rows per thread; the row counts leave partial tiles and partial warps)."""
     import ctypes
     lib = pkg.load_library()
     fp64 = int(dtype == np.float64)
@@ -76,7 +77,7 @@ def test_apply_both_tile_shapes(cuda, pkg, oracle, dtype, shape):
     assert lib.symeig_apply_tuning(fp64, ctypes.byref(v), 1) == 0
     try:
         rng = np.random.default_rng(99 + shape)
-        for (m, n, k) in [(33, 70, 64), (100, 129, 130), (7, 20, 5)]:
+        for (m, n, k) in [(33, 70, 64), (100, 129, 130), (7, 20, 5), (77, 40, 64)]:
             g = rotation_grid(pkg, rng, n, k, dtype)
             A = np.asfortranarray((rng.random((m, n)) * 2 - 1).astype(dtype))
             ref = A.copy(order="F")

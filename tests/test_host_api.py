@@ -114,3 +114,23 @@ def test_dense_entry_points_validate_arguments(pkg):
     assert lib.symeig_orgtr_f64(None, 4, buf, 4, buf, buf, 4) == 5
     assert lib.symeig_syev_f64(None, 4, buf, 4, buf, buf, 4, ctypes.byref(c32), ctypes.byref(c64)) == 5
     assert lib.symeig_sytrd_f64_dev(None, 4, buf, 4, buf, buf, buf) == 5
+
+
+def test_apply_tuning_shapes_per_precision(pkg):
+    """symeig_apply_tuning keeps the tile shape per precision: FP64 has shapes 0-1, FP32 0-3
+    (2 and 3 hold two rows per thread); out-of-range shapes are refused and leave it as it was.
+    Setting the shape touches no device."""
+    import ctypes
+    lib = pkg.load_library()
+    v = ctypes.c_int32()
+    assert lib.symeig_apply_tuning(1, ctypes.byref(v), 0) == 0 and v.value == 0
+    assert lib.symeig_apply_tuning(0, ctypes.byref(v), 0) == 0 and v.value == 2
+    for fp64, bad in ((1, 2), (1, -1), (0, 4)):
+        v = ctypes.c_int32(bad)
+        assert lib.symeig_apply_tuning(fp64, ctypes.byref(v), 1) == 2      # SYMEIG_ERR_SIZE
+    v = ctypes.c_int32(3)
+    assert lib.symeig_apply_tuning(0, ctypes.byref(v), 1) == 0
+    assert lib.symeig_apply_tuning(0, ctypes.byref(v), 0) == 0 and v.value == 3
+    v = ctypes.c_int32(2)
+    assert lib.symeig_apply_tuning(0, ctypes.byref(v), 1) == 0
+    assert lib.symeig_apply_tuning(1, ctypes.byref(v), 0) == 0 and v.value == 0
