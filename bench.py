@@ -58,8 +58,9 @@ def parse_args():
     p.add_argument("--form", choices=["canonical", "scaled"], default="canonical",
                    help="FP64 apply form: canonical rotations (4 FP64 ops per rotation-row) or the "
                         "scaled form (2 FMAs per rotation-row; a few ulps from canonical)")
-    p.add_argument("--chase-mode", type=int, choices=[0, 1, 2], default=0,
-                   help="solve workload: 0 Newton-form two-warp chase, 1 reference form, 2 Newton + redo")
+    p.add_argument("--chase-mode", type=int, choices=[0, 1, 2, 3], default=0,
+                   help="solve workload: 0 Newton-form two-warp chase, 1 reference form, 2 Newton + redo, "
+                        "3 multishift batches")
     p.add_argument("--count", type=int, default=4096, help="batched workload: number of tridiagonals")
     p.add_argument("--loop-sample", type=int, default=16,
                    help="batched workload: matrices timed one launch per matrix (extrapolated by sum n^2)")
@@ -512,6 +513,7 @@ def run_solve(args):
         "chase_us_per_rotation": round(st["chase_ms"] * 1e3 / max(st["rotations"], 1), 4),
         "givens_gflops_apply": round(6.0 * n * st["rotations"] / (st["apply_ms"] * 1e-3) / 1e9, 1),
         "early_flushes": st["early_flushes"], "redone_sweeps": st["redone_sweeps"],
+        "bulge_batches": st["bulge_batches"],
         "errors": {"eig_max_abs_vs_lapack": eig_err, "eig_bound_10n_eps_normT": 10 * n * eps * normT,
                    "resid_rel": resid, "orth": orth, "bound_10n_eps": 10 * n * eps},
         "clocks": clk.summary(),

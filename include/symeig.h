@@ -52,6 +52,7 @@ typedef struct {
     double  wave_kernel_ms;  /* their summed device time (only with kernel timing on)     */
     int64_t device_errors;   /* nonzero if a kernel's bounded wait gave up (sticky)        */
     int64_t redone_sweeps;   /* chase sweeps run again in the reference form (see below)  */
+    int64_t bulge_batches;   /* multishift batches the chase ran (chase mode 3)           */
 } symeig_stats;
 
 /* Create a handle bound to CUDA device `device`.  Replaces nothing in the reference (the
@@ -71,13 +72,22 @@ int symeig_get_stats(symeig_handle h, symeig_stats* out);
  * 137-139), whose wave order differs from the chase's order when a split block re-merges
  * within a flush (Q then loses accuracy in the reference too).  No reference counterpart. */
 int symeig_set_exact_order(symeig_handle h, int32_t exact_order);
-/* How the chase kernel computes its rotations; every mode gives the same bits.
+/* How the chase kernel computes its rotations.  Modes 0-2 give the same bits: the reference's
+ * sweep sequence and rotations.
  * 0 (default): two warps, givensAlgorithm's plain branch from FMA-only Newton steps whose
  *   rounding is proved step by step; a sweep with an unproved step is restored and run again
  *   in the reference form (counted in redone_sweeps).
  * 1: the reference form (correctly rounded division and square root) on one thread.
  * 2: as 0, but every sweep is then redone in the reference form (exercises the restore).
- * No reference counterpart. */
+ * 3: multishift.  Where a block has at least 2 * 64 rows and room for several layers, the
+ *   chase runs a batch of up to 32 sweeps whose shifts are the eigenvalues of the block's
+ *   trailing square (one per sweep), as bulges chased concurrently on separate SMs, each a
+ *   fixed number of rows behind the one before.  The deflation test, the capacity rule and
+ *   the rotation placement are those of a sequence of single sweeps with those shifts; shorter
+ *   blocks take the Wilkinson single sweep of mode 0.  Results meet the same error bounds as
+ *   the reference (eigenvalues within 10 n eps ||T||, residual and orthogonality within
+ *   10 n eps) but are not the reference's bits; the sweep count is higher (about 1.2-1.6x),
+ *   the chase time far lower.  No reference counterpart. */
 int symeig_set_chase_mode(symeig_handle h, int32_t mode);
 /* Arithmetic form of the FP64 bulk apply (symeig_apply_givens_f64*, and the qr driver's
  * apply with FP64 Q).  0 (default): every rotation as the reference's rmul!, four FP64

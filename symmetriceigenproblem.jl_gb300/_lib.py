@@ -76,7 +76,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("iterations", c_i64), ("flushes", c_i64), ("rotations", c_i64),
                 ("applied_rotation_rows", c_i64), ("chase_ms", c_dbl), ("apply_ms", c_dbl),
                 ("total_ms", c_dbl), ("early_flushes", c_i64), ("wave_launches", c_i64),
-                ("wave_kernel_ms", c_dbl), ("device_errors", c_i64), ("redone_sweeps", c_i64)]
+                ("wave_kernel_ms", c_dbl), ("device_errors", c_i64), ("redone_sweeps", c_i64),
+                ("bulge_batches", c_i64)]
 
     def as_dict(self) -> dict:
         return {f: getattr(self, f) for f, _ in self._fields_}

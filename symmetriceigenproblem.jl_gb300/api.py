@@ -192,8 +192,9 @@ def qr_algorithm_(H: SymTridiagonal, Q=None, max_layers: int = 128, tol: float |
     (c,s) rounded to float).  exact_order=False places rotations in the grid as the reference
     does (grid[i, ++layer_thickness[i]]), which loses accuracy in Q when a split block
     re-merges within a flush; the default places each sweep at one layer so Q is exact.
-    chase_mode selects how the chase computes rotations (symeig_set_chase_mode); every mode
-    gives the same bits.  apply_form=1 applies each flush to an FP64 Q in the scaled form
+    chase_mode selects how the chase computes rotations (symeig_set_chase_mode); modes 0-2
+    give the reference's bits, mode 3 (multishift batches of concurrent bulges) meets the
+    reference's error bounds with a different sweep sequence.  apply_form=1 applies each flush to an FP64 Q in the scaled form
     (symeig_set_apply_form)."""
     n = H.n
     tol = EPS64 if tol is None else float(tol)

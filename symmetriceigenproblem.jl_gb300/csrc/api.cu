@@ -55,7 +55,7 @@ struct symeig_context {
     cudaEvent_t ev_chased[2] = {nullptr, nullptr};
     cudaEvent_t ev_consumed[2] = {nullptr, nullptr};
     cudaEvent_t ev_main = nullptr;
-    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs, bak, rot, dense, dense_io;
+    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs, bak, rot, dense, dense_io, bulge;
     int* derr = nullptr;   // device error word of the wave kernels (bounded waits)
     int32_t exact_order = 1;  // rotation placement of the qr driver
     int32_t chase_mode = 0;   // symeig_set_chase_mode
@@ -203,6 +203,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     }
     CK(h->state.ensure(sizeof(ChaseState)));
     CK(h->bak.ensure((size_t)2 * n * sizeof(double)));
+    CK(h->bulge.ensure(sizeof(BulgeScratch)));
 
     ChaseState init{};
     init.n = n;
@@ -245,12 +246,25 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
         cudaEvent_t c0 = timing_event(h, tev++), c1 = timing_event(h, tev++);
         if (!c0 || !c1) return SYMEIG_ERR_CUDA;
         CK(cudaEventRecord(c0, cs));
+        BulgeScratch* bsc = (BulgeScratch*)h->bulge.ptr;
         CK(launch_chase(dstate, d, e, (double*)h->grid[b].ptr, (int32_t*)h->thick[b].ptr,
-                        (int32_t*)h->place[b].ptr, (double*)h->bak.ptr, cs));
+                        (int32_t*)h->place[b].ptr, (double*)h->bak.ptr, bsc, cs));
         CK(cudaEventRecord(c1, cs));
         CK(cudaMemcpyAsync(h->h_state, dstate, sizeof(ChaseState), cudaMemcpyDeviceToHost, cs));
         CK(cudaEventRecord(h->ev_chased[b], cs));
         CK(cudaEventSynchronize(h->ev_chased[b]));
+        // chase_mode 3: each multishift batch runs in its own cooperative launch, after which
+        // the chase kernel resumes the flush
+        while (h->h_state->status == CHASE_BATCH) {
+            CK(launch_bulge_batch(dstate, d, e, (double*)h->grid[b].ptr, (const int32_t*)h->thick[b].ptr,
+                                  bsc, h->derr, h->h_state->b_bulges, cs));
+            CK(launch_chase(dstate, d, e, (double*)h->grid[b].ptr, (int32_t*)h->thick[b].ptr,
+                            (int32_t*)h->place[b].ptr, (double*)h->bak.ptr, bsc, cs));
+            CK(cudaEventRecord(c1, cs));
+            CK(cudaMemcpyAsync(h->h_state, dstate, sizeof(ChaseState), cudaMemcpyDeviceToHost, cs));
+            CK(cudaEventRecord(h->ev_chased[b], cs));
+            CK(cudaEventSynchronize(h->ev_chased[b]));
+        }
         float ms_chase = 0.f;
         CK(cudaEventElapsedTime(&ms_chase, c0, c1));
         chase_ms += ms_chase;
@@ -298,6 +312,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     h->stats.rotations = fin.total_rotations;
     h->stats.early_flushes = fin.early_flushes;
     h->stats.redone_sweeps = fin.redone_sweeps;
+    h->stats.bulge_batches = fin.batches;
     h->stats.chase_ms = chase_ms;
     h->stats.apply_ms = apply_ms;
     h->stats.total_ms =
@@ -583,7 +598,7 @@ int symeig_set_exact_order(symeig_handle h, int32_t exact_order)
 int symeig_set_chase_mode(symeig_handle h, int32_t mode)
 {
     if (!h) return SYMEIG_ERR_HANDLE;
-    if (mode < 0 || mode > 2) return SYMEIG_ERR_SIZE;
+    if (mode < 0 || mode > 3) return SYMEIG_ERR_SIZE;
     h->chase_mode = mode;
     return SYMEIG_OK;
 }

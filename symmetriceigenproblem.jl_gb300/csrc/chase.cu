@@ -286,6 +286,235 @@ __device__ __forceinline__ int32_t warp_max(int32_t v)
     return v;
 }
 
+// ---- multishift batches (chase_mode 3) -----------------------------------------------------
+//
+// Shifts of a batch of nb bulges over a block ending at row `to` (1-based): the eigenvalues of
+// the block's trailing nb x nb principal submatrix, ascending, by bisection on Sturm counts.
+// The submatrix is scaled by an exact power of two to max |entry| in [0.5, 1) and the counts
+// run in FP32: a shift only steers convergence (the deflation test and the sweeps stay FP64).
+// Lane l < nb finds the l-th eigenvalue.  All 32 lanes of warp 0 call it; sd, se2 and sea
+// are 32-entry shared arrays.
+__device__ void batch_shifts(const double* __restrict__ dv, const double* __restrict__ ev,
+                             int64_t to, int nb, double* __restrict__ shifts, float* sd, float* se2,
+                             float* sea)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t r0 = to - nb;  // 0-based first row of the submatrix
+    const double dq = lane < nb ? dv[r0 + lane] : 0.0;
+    const double eq = lane < nb - 1 ? ev[r0 + lane] : 0.0;
+    double mx = fmax(fabs(dq), fabs(eq));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if (!(mx > 0.0) || !isfinite(mx)) {
+        // a zero block is already diagonal; a non-finite one is left to the sweep
+        if (lane < nb) shifts[lane] = dq;
+        __syncwarp();
+        return;
+    }
+    int ex;
+    frexp(mx, &ex);
+    const float df = (float)ldexp(dq, -ex), ef = (float)ldexp(eq, -ex);
+    sd[lane] = df;
+    se2[lane] = ef * ef;
+    sea[lane] = fabsf(ef);
+    __syncwarp();
+    // Gershgorin interval of the submatrix
+    float lo = 3.0f, hi = -3.0f;
+    if (lane < nb) {
+        const float rad = (lane >= 1 ? sea[lane - 1] : 0.0f) + (lane < nb - 1 ? sea[lane] : 0.0f);
+        lo = df - rad;
+        hi = df + rad;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    }
+    lo -= 1e-6f;
+    hi += 1e-6f;
+    constexpr float kPiv = 1e-30f;
+    for (int it = 0; it < 40; ++it) {
+        const float mid = 0.5f * (lo + hi);
+        if (!(mid > lo && mid < hi)) break;
+        // number of eigenvalues below mid (negative pivots of T - mid I = L D L^T)
+        float q = sd[0] - mid;
+        int cnt = q < 0.0f;
+        for (int i = 1; i < nb; ++i) {
+            if (fabsf(q) < kPiv) q = -kPiv;
+            q = (sd[i] - mid) - se2[i - 1] / q;
+            cnt += q < 0.0f;
+        }
+        if (cnt > lane) hi = mid;
+        else lo = mid;
+    }
+    if (lane < nb) shifts[lane] = ldexp((double)(0.5f * (lo + hi)), ex);
+    __syncwarp();
+}
+
+// The bulges of a batch.  Bulge j (CTA j) runs the two-warp sweep of sweep_nr_2w (same split,
+// mailbox and barriers) with shift shifts[j] over the batch's block, one step behind another
+// bulge's stores: step k of a sweep stores dv[k-1] and ev[k-2] (0-based; its last step also
+// dv[k] and ev[k-1]), so before its loads for step i+1 (dv[i+1], ev[i+1]) bulge j needs bulge
+// j-1 through step min(i+3, to-1).  The helper warp's store thread releases the bulge's
+// progress every kProgEvery steps and at its last step (st.release.gpu); the next bulge's
+// warps read it with ld.acquire.gpu only when the value they hold is too small, and read
+// dv/ev through L2 (ld.global.cg), never from a stale L1 line.  Bulge j waits only for bulge
+// j-1 and the CTAs are co-resident (one cooperative launch), so the waits form one chain that
+// starts at bulge 0, which waits for none.  Every wait is bounded (about 2 s of SM clock): one
+// that gives up sets the device error word, and the warp carries on without waiting, so the
+// two warps' barrier protocol still completes; the call then reports the error.
+// The rotation is givens_nr_core (reference form out of its range) without the rounding
+// proof: the batch is not the reference's sweep sequence, so there are no bits to match.
+constexpr int kProgEvery = 8;
+
+__device__ __forceinline__ long long ld_acquire_gpu(const long long* p)
+{
+    long long v;
+    asm volatile("ld.acquire.gpu.global.s64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release_gpu(long long* p, long long v)
+{
+    asm volatile("st.release.gpu.global.s64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Every lane polls with its own acquire load, and the warp moves on together: when all lanes
+// saw the value needed (it keeps their minimum, which every lane has synchronised with, the
+// progress word only growing) or when any lane's wait ran out.
+struct PipeWait {
+    const long long* pred;  // progress word of the bulge ahead; null for bulge 0
+    int* err;
+    long long known;        // the smallest value the warp's lanes last read (warp-uniform)
+    __device__ __forceinline__ void until(long long need)
+    {
+        if (pred == nullptr || known >= need) return;
+        const long long t0 = clock64();
+        for (;;) {
+            long long v = ld_acquire_gpu(pred);
+            if (__all_sync(0xffffffffu, v >= need)) {
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) v = min(v, __shfl_xor_sync(0xffffffffu, v, o));
+                known = v;
+                return;
+            }
+            const bool give_up = *(volatile int*)err != 0 || clock64() - t0 > 4000000000LL;
+            if (__any_sync(0xffffffffu, give_up)) {
+                if ((threadIdx.x & 31) == 0) atomicExch(err, 1);
+                known = 0x7fffffffffffffffLL;  // stop waiting for the rest of the sweep
+                return;
+            }
+        }
+    }
+};
+
+__device__ void sweep_bulge_2w(double* __restrict__ dv, double* __restrict__ ev, int64_t from,
+                               int64_t to, double mu, double* __restrict__ grid,
+                               const int32_t* __restrict__ thick, int64_t rows, int32_t layer,
+                               int32_t jofs, double nz, NrMail* mail, PipeWait pw,
+                               long long* __restrict__ my_prog)
+{
+    const int warp = threadIdx.x >> 5;
+    const bool lead = (threadIdx.x & 31) == 0;
+    pw.until(min(from + 2, to - 1));
+    const double H11 = __ldcg(dv + from - 1), H21 = __ldcg(ev + from - 1);
+    if (warp == 0) {
+        double f = __dsub_rn(H11, mu), g = H21, gg = mulz(H21, H21, nz);
+        double B11 = H11, B21 = H21;
+        double B22n = __ldcg(dv + from);
+        double B23n = (from + 2 <= to) ? __ldcg(ev + from) : 0.0;
+        for (int64_t i = from; i <= to - 1; ++i) {
+            const double B22 = B22n, B23 = B23n;
+            pw.until(min(i + 3, to - 1));
+            if (i + 1 <= to - 1) B22n = __ldcg(dv + i + 1);
+            if (i + 3 <= to) B23n = __ldcg(ev + i + 1);
+            const NrRot o = givens_nr_core(f, g, gg, nz);
+            double c = o.c, s = o.s, r = o.r;
+            if (!nr_in_range(f, g)) givens_fast(f, g, c, s, r, nz);
+            if (i > from) {
+                nb_sync(kBarB);
+                const NrMail& pv = mail[(i - 1) & 1];
+                B11 = pv.b22pp;
+                B21 = pv.e_next;
+            }
+            NrMail& mb = mail[i & 1];
+            mb.c = c; mb.s = s; mb.r = r;
+            nb_arrive(kBarCS);
+            const double B11p = __fma_rn(c, B11, mulz(s, B21, nz));
+            const double B12p = __fma_rn(c, B21, mulz(s, B22, nz));
+            f = __fma_rn(B12p, c, -mulz(B11p, s, nz));
+            g = (i + 2 <= to) ? mulz(s, B23, nz) : 0.0;
+            gg = mulz(g, g, nz);
+        }
+    } else {
+        double B11 = H11, B21 = H21;
+        double B22n = __ldcg(dv + from);
+        double B23n = (from + 2 <= to) ? __ldcg(ev + from) : 0.0;
+        int32_t thn = layer <= 0 ? thick[from - 1] : 0;
+        for (int64_t i = from; i <= to - 1; ++i) {
+            const double B22 = B22n, B23 = B23n;
+            const int32_t th = thn;
+            pw.until(min(i + 3, to - 1));
+            if (i + 1 <= to - 1) B22n = __ldcg(dv + i + 1);
+            if (i + 3 <= to) B23n = __ldcg(ev + i + 1);
+            if (layer <= 0 && i + 1 <= to - 1) thn = thick[i];
+            nb_sync(kBarCS);
+            const NrMail& mb = mail[i & 1];
+            const double c = mb.c, s = mb.s, r = mb.r;
+            const double e_next = (i + 2 <= to) ? mulz(c, B23, nz) : 0.0;
+            const double sB21 = mulz(s, B21, nz);
+            const double B21p = __fma_rn(c, B21, -mulz(s, B11, nz));
+            const double B22p = __fma_rn(c, B22, -sB21);
+            const double B22pp = __fma_rn(B22p, c, -mulz(B21p, s, nz));
+            if (i < to - 1) {
+                NrMail& mo = mail[i & 1];
+                mo.b22pp = B22pp;
+                mo.e_next = e_next;
+                nb_arrive(kBarB);
+            }
+            const double B11p = __fma_rn(c, B11, sB21);
+            const double B12p = __fma_rn(c, B21, mulz(s, B22, nz));
+            const double B11pp = __fma_rn(B11p, c, mulz(B12p, s, nz));
+            if (lead) {
+                dv[i - 1] = B11pp;
+                if (i > from) ev[i - 2] = r;
+                const int32_t L = layer > 0 ? layer : th + 1 + jofs;
+                *reinterpret_cast<double2*>(grid + 2 * ((i - 1) + (int64_t)(L - 1) * rows)) =
+                    make_double2(c, s);
+                if (i == to - 1) {
+                    dv[i] = B22pp;
+                    ev[i - 1] = __fma_rn(B12p, c, -mulz(B11p, s, nz));
+                }
+                if (i == to - 1 || (i - from) % kProgEvery == kProgEvery - 1) st_release_gpu(my_prog, i);
+            }
+            B11 = B22pp;
+            B21 = e_next;
+        }
+    }
+}
+
+// One CTA of two warps per bulge; dynamic shared memory (kBatchSmem) keeps one CTA per SM, so
+// no two bulges share an SM's FP64 unit.
+constexpr int kBatchSmem = 120 * 1024;
+
+__global__ void __launch_bounds__(64, 1)
+bulge_batch_kernel(const ChaseState* __restrict__ st, double* __restrict__ dv,
+                   double* __restrict__ ev, double* __restrict__ grid,
+                   const int32_t* __restrict__ thick, BulgeScratch* __restrict__ bs,
+                   int* __restrict__ err)
+{
+    __shared__ NrMail mail[2];
+    const int j = blockIdx.x;
+    const int32_t nb = st->b_bulges;
+    if (j >= nb) return;
+    const int64_t n = st->n, from = st->b_from, to = st->b_to;
+    const int64_t rows = n > 1 ? n - 1 : 1;
+    const int32_t L0 = st->b_layer0;
+    PipeWait pw{j > 0 ? &bs->prog[j - 1] : nullptr, err, -1};
+    sweep_bulge_2w(dv, ev, from, to, bs->shifts[j], grid, thick, rows, L0 > 0 ? L0 + j : 0, j,
+                   st->neg_zero, mail, pw, &bs->prog[j]);
+}
+
 // One flush: the reference's inner loop from `to = last_block_ends_at` until the matrix is
 // split into converged parts, every block has reached max_layers, or iter > maxiter.
 // Warp 0 runs the control flow and the O(n) scans with ballots; each sweep runs on both
@@ -304,17 +533,19 @@ struct Decision {
     int64_t from, to;
     double mu;
     int32_t layer;
-    int32_t action;  // 0 stop, 1 sweep, 2 no sweep this iteration
+    int32_t action;  // 0 stop, 1 sweep, 2 no sweep this iteration, 3 multishift batch
+    int32_t bulges;  // action 3: sweeps of the batch
 };
 
 __global__ void __launch_bounds__(64, 1)
 chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __restrict__ ev,
              double* __restrict__ grid, int32_t* __restrict__ thick, int32_t* __restrict__ place,
-             double* __restrict__ bak)
+             double* __restrict__ bak, BulgeScratch* __restrict__ bs)
 {
     __shared__ NrMail mail[2];
     __shared__ Decision dec;
     __shared__ int32_t fail;
+    __shared__ float ms_d[32], ms_e2[32], ms_ea[32];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int64_t n = st->n;
@@ -331,21 +562,37 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
     const int64_t rows = n > 1 ? n - 1 : 1;
     int64_t redone = 0;
 
-    for (int64_t q = threadIdx.x; q < n; q += 64) {
-        thick[q] = 0;
-        place[q] = 0;
+    // chase_mode 3 returns to the host for each multishift batch; the launch after the batch
+    // resumes the flush where it stopped, first recording the batch in thick/place: every
+    // index of its block got one layer per bulge (bulge j at layer thick + 1 + j, or at the
+    // exact-order layer b_layer0 + j).
+    const bool resume = st->resume != 0;
+    if (!resume) {
+        for (int64_t q = threadIdx.x; q < n; q += 64) {
+            thick[q] = 0;
+            place[q] = 0;
+        }
+    } else {
+        const int32_t nbk = st->b_bulges, L0 = st->b_layer0;
+        for (int64_t q = st->b_from - 1 + threadIdx.x; q < st->b_to - 1; q += 64) {
+            const int32_t t = thick[q] + nbk;
+            thick[q] = t;
+            place[q] = L0 > 0 ? L0 + nbk - 1 : t;
+        }
     }
     if (threadIdx.x == 0) fail = 0;
     __syncthreads();
 
-    bool did = false;
-    int64_t rotations = 0, min_from = n + 1, max_to = 0, early = 0;
+    bool did = resume && st->r_did != 0;
+    int64_t rotations = resume ? st->r_rotations : 0, min_from = resume ? st->r_min_from : n + 1;
+    int64_t max_to = resume ? st->r_max_to : 0, early = resume ? st->r_early : 0;
     int32_t status = CHASE_RUNNING;
-    int64_t to = lbe;
+    int64_t to = resume ? st->r_to : lbe;
+    Decision last{};
 
     for (;;) {
         if (warp == 0) {
-            Decision d{0, 0, 0.0, 0, 2};
+            Decision d{0, 0, 0.0, 0, 2, 1};
             if (iter > maxiter) {
                 status = CHASE_MAXITER;
                 d.action = 0;
@@ -395,14 +642,29 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
                             }
                         }
                         if (go) {
-                            d.mu = wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
+                            // mode 3: as many bulges as the block's length, its layer room
+                            // (the capacity rule of that many single sweeps) and maxiter allow
+                            int64_t nbl = 1;
+                            if (mode == 3) {
+                                int64_t cap = (int64_t)max_layers - mx;
+                                if (exact) cap = min(cap, (int64_t)grid_layers - layer + 1);
+                                nbl = min(min((int64_t)kMaxBulges, (to - from + 1) / kRowsPerBulge), cap);
+                                nbl = min(nbl, maxiter - iter + 1);
+                            }
+                            if (nbl >= 2) {
+                                batch_shifts(dv, ev, to, (int)nbl, bs->shifts, ms_d, ms_e2, ms_ea);
+                                d.bulges = (int32_t)nbl;
+                                d.action = 3;
+                            } else {
+                                d.mu = wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
+                                d.action = 1;
+                            }
                             d.from = from;
                             d.to = to;
                             d.layer = layer;
-                            d.action = 1;
                             did = true;
-                            iter += 1;
-                            rotations += to - from;
+                            iter += nbl >= 2 ? nbl : 1;
+                            rotations += (nbl >= 2 ? nbl : 1) * (to - from);
                             min_from = min(min_from, from);
                             max_to = max(max_to, to);
                         }
@@ -414,6 +676,8 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
         }
         __syncthreads();
         const Decision d = dec;
+        last = d;
+        if (d.action == 3) break;  // the batch runs in its own launch
         if (d.action == 1) {
             // entries the sweep may change: dv[from-1 .. to-1], ev[from-1 .. to-2] (0-based)
             const int64_t q0 = d.from - 1, q1 = d.to - 1;
@@ -453,6 +717,29 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
         if (d.action == 0) break;  // both warps leave on the same decision
     }
 
+    if (last.action == 3) {
+        // hand the batch to the host: its block, its layers, and the loop state to resume
+        for (int q = threadIdx.x; q < last.bulges; q += 64) bs->prog[q] = -1;
+        if (threadIdx.x == 0) {
+            st->status = CHASE_BATCH;
+            st->resume = 1;
+            st->b_bulges = last.bulges;
+            st->b_from = last.from;
+            st->b_to = last.to;
+            st->b_layer0 = last.layer;
+            st->r_did = did ? 1 : 0;
+            st->r_to = to;
+            st->r_rotations = rotations;
+            st->r_min_from = min_from;
+            st->r_max_to = max_to;
+            st->r_early = early;
+            st->iter = iter;
+            st->last_block_ends_at = lbe;
+            st->redone_sweeps += redone;
+            st->batches += 1;
+        }
+        return;
+    }
     if (warp == 0) {
         int32_t kmax = 0;
         for (int64_t q = lane; q < n; q += 32) kmax = max(kmax, place[q]);
@@ -469,6 +756,7 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
             st->total_rotations += rotations;
             st->early_flushes += early;
             st->redone_sweeps += redone;
+            st->resume = 0;
         }
     }
 }
@@ -607,10 +895,23 @@ cudaError_t launch_get_rotation(int64_t count, const double* f, const double* g,
 }
 
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
-                         int32_t* place, double* bak, cudaStream_t stream)
+                         int32_t* place, double* bak, BulgeScratch* bs, cudaStream_t stream)
 {
-    chase_kernel<<<1, 64, 0, stream>>>(state, d, e, grid, thick, place, bak);
+    chase_kernel<<<1, 64, 0, stream>>>(state, d, e, grid, thick, place, bak, bs);
     return cudaGetLastError();
+}
+
+cudaError_t launch_bulge_batch(const ChaseState* state, double* d, double* e, double* grid,
+                               const int32_t* thick, BulgeScratch* bs, int* err, int32_t bulges,
+                               cudaStream_t stream)
+{
+    if (bulges < 2 || bulges > kMaxBulges) return cudaErrorInvalidValue;
+    cudaError_t ce = cudaFuncSetAttribute(bulge_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          kBatchSmem);
+    if (ce != cudaSuccess) return ce;
+    void* args[] = {(void*)&state, (void*)&d, (void*)&e, (void*)&grid, (void*)&thick, (void*)&bs, (void*)&err};
+    return cudaLaunchCooperativeKernel((const void*)bulge_batch_kernel, dim3((unsigned)bulges), dim3(64), args,
+                                       (size_t)kBatchSmem, stream);
 }
 
 cudaError_t launch_chase_batched(const BatchMat* mats, const int32_t* order, int32_t count,

@@ -52,6 +52,18 @@ enum ChaseStatus : int32_t {
     CHASE_CONVERGED = 1,   // the flush recorded no rotation: the reference's `!did_a_thing && break`
     CHASE_MAXITER   = 2,   // iter > maxiter: the reference returns (H, false, iter)
     CHASE_FLUSH     = 3,   // rotations recorded; apply them, then chase again
+    CHASE_BATCH     = 4,   // a multishift batch is pending: run it, then resume the flush
+};
+
+// Multishift batches (chase_mode 3): at most kMaxBulges bulges per batch, and a batch over a
+// block of len rows has at most len / kRowsPerBulge bulges.
+constexpr int kMaxBulges = 32;
+constexpr int kRowsPerBulge = 64;
+
+// Device scratch of a batch: the bulges' shifts and their progress words.
+struct BulgeScratch {
+    double shifts[kMaxBulges];
+    long long prog[kMaxBulges];  // last step whose stores a bulge has released
 };
 
 struct ChaseState {
@@ -77,6 +89,14 @@ struct ChaseState {
                                  // thread, 2 Newton form with every sweep redone (tests)
     int32_t pad0;
     int64_t redone_sweeps;       // sweeps run again in the reference form (cumulative)
+    // chase_mode 3: the pending batch and the flush's loop state to resume after it
+    int32_t resume;              // 1: the next chase launch continues the flush after a batch
+    int32_t b_bulges;            // bulges of the pending batch
+    int64_t b_from, b_to;        // 1-based block the batch sweeps
+    int32_t b_layer0;            // exact-order layer of bulge 0, or 0 (the reference's placement)
+    int32_t r_did;
+    int64_t r_to, r_rotations, r_min_from, r_max_to, r_early;
+    int64_t batches;             // batches run (cumulative)
 };
 
 // ---- launch helpers (defined in the .cu files) ------------------------------------------
@@ -132,7 +152,12 @@ cudaError_t launch_tridiag_unscale(double* A, int64_t lda, int64_t n, double* d,
 cudaError_t launch_get_rotation(int64_t count, const double* f, const double* g, double* c,
                                 double* s, double* r, int32_t form, cudaStream_t stream);
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
-                         int32_t* place, double* bak, cudaStream_t stream);
+                         int32_t* place, double* bak, BulgeScratch* bs, cudaStream_t stream);
+// The pending multishift batch of `state` (status CHASE_BATCH): `bulges` CTAs of two warps in
+// one cooperative launch, one bulge each.  A bounded wait that gives up sets *err.
+cudaError_t launch_bulge_batch(const ChaseState* state, double* d, double* e, double* grid,
+                               const int32_t* thick, BulgeScratch* bs, int* err, int32_t bulges,
+                               cudaStream_t stream);
 
 // One matrix of a batch: size and offsets into the packed arrays (elements, not bytes).
 struct BatchMat {

@@ -1,0 +1,151 @@
+"""The multishift chase (chase_mode 3): batches of up to 32 sweeps whose shifts are the
+eigenvalues of the block's trailing square, chased as concurrent bulges.  It is not the
+reference's sweep sequence, so it is checked against the error bounds the reference meets
+(eigenvalues within 10 n eps ||T|| of LAPACK, ||TQ - QD||_F / ||T||_F and ||Q^T Q - I||_F
+within 10 n eps), and, where no block is long enough for a batch (n < 128), against the
+oracle bit for bit."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+from scipy.linalg import eigh_tridiagonal
+
+from test_qr_gpu import tridiag
+
+pytestmark = pytest.mark.gpu
+
+EPS = np.finfo(np.float64).eps
+
+
+def errors(d, e, lam, Q):
+    """(eigenvalue error / (10 n eps ||T||), residual / (10 n eps), orthogonality / (10 n eps))."""
+    n = d.size
+    ref = eigh_tridiagonal(d, e, eigvals_only=True)
+    normT = float(np.max(np.abs(ref)))
+    eig = float(np.max(np.abs(np.sort(lam) - ref))) / (10 * n * EPS * normT)
+    if Q is None:
+        return eig, 0.0, 0.0
+    TQ = d[:, None] * Q
+    TQ[:-1] += e[:, None] * Q[1:]
+    TQ[1:] += e[:, None] * Q[:-1]
+    normT_F = np.sqrt(float((d * d).sum() + 2 * (e * e).sum()))
+    res = float(np.linalg.norm(TQ - Q * lam[None, :])) / normT_F / (10 * n * EPS)
+    G = Q.T @ Q - np.eye(n)
+    orth = float(np.linalg.norm(G)) / (10 * n * EPS)
+    return eig, res, orth
+
+
+def solve(pkg, d, e, Q="eye", **kw):
+    n = d.size
+    H = pkg.SymTridiagonal(d.copy(), e.copy())
+    if isinstance(Q, str):
+        Q = np.asfortranarray(np.eye(n))
+    h = pkg.Handle(0)
+    try:
+        _, conv, it = pkg.qr_algorithm_(H, Q, handle=h, chase_mode=3, **kw)
+        st = h.stats()
+    finally:
+        h.close()
+    return H.dv, Q, conv, it, st
+
+
+@pytest.mark.parametrize("kind,n", [("C", 100), ("A", 127), ("split", 120), ("B", 64)])
+def test_multishift_short_blocks_are_the_reference(cuda, pkg, oracle, kind, n):
+    """No block below 2 x 64 rows takes a batch: mode 3 is then mode 0, the oracle's bits."""
+    d, e = tridiag(kind, n, seed=n)
+    od, oe, oQ = d.copy(), e.copy(), np.asfortranarray(np.eye(n))
+    conv_o, it_o, _, _ = oracle.qr_algorithm(od, oe, oQ)
+    lam, Q, conv, it, st = solve(pkg, d, e)
+    assert st["bulge_batches"] == 0
+    assert (conv, it) == (conv_o, it_o)
+    assert np.array_equal(lam, od) and np.array_equal(Q, oQ)
+
+
+MS_CASES = [("A", 2000), ("B", 1500), ("C", 777), ("split", 900), ("graded", 600), ("A", 4097)]
+
+
+@pytest.mark.parametrize("kind,n", MS_CASES)
+def test_multishift_error_bounds(cuda, pkg, kind, n):
+    d, e = tridiag(kind, n, seed=n + 11)
+    lam, Q, conv, it, st = solve(pkg, d, e)
+    assert conv
+    assert st["bulge_batches"] > 0
+    assert st["device_errors"] == 0
+    eig, res, orth = errors(d, e, lam, Q)
+    assert eig <= 1.0 and res <= 1.0 and orth <= 1.0, (eig, res, orth)
+
+
+@pytest.mark.parametrize("kind,n", MS_CASES)
+def test_multishift_reference_placement(cuda, pkg, kind, n):
+    """With the reference's grid placement (exact_order=False) the eigenvalues and the
+    orthogonality of Q meet the bounds.  The residual is not asserted: that placement applies
+    a flush in an order that differs from the chase's once a split block re-merges, and the
+    reference's own sweep sequence (the oracle, mode 0) then misses it too, e.g. by 1.1e3 x
+    the bound on case B, n = 1500 and by 1.3e4 x on the split case, n = 900."""
+    d, e = tridiag(kind, n, seed=n + 11)
+    lam, Q, conv, it, st = solve(pkg, d, e, exact_order=False)
+    assert conv and st["bulge_batches"] > 0 and st["device_errors"] == 0
+    eig, res, orth = errors(d, e, lam, Q)
+    assert eig <= 1.0 and orth <= 1.0, (eig, res, orth)
+
+
+@pytest.mark.parametrize("max_layers", [2, 3, 8, 40])
+def test_multishift_small_max_layers(cuda, pkg, max_layers):
+    """The layer room caps the bulges of a batch (max_layers = 2: two per batch at most)."""
+    n = 1100
+    d, e = tridiag("C", n, seed=5)
+    lam, Q, conv, it, st = solve(pkg, d, e, max_layers=max_layers)
+    assert conv and st["bulge_batches"] > 0
+    eig, res, orth = errors(d, e, lam, Q)
+    assert eig <= 1.0 and res <= 1.0 and orth <= 1.0, (eig, res, orth)
+
+
+def test_multishift_eigenvalues_only_and_rectangular_q(cuda, pkg):
+    """Q = None runs the chase alone; a rectangular Q (m x n) receives the same rotations as
+    the identity does, so it ends as Q0 * V."""
+    n, m = 1300, 257
+    d, e = tridiag("B", n, seed=21)
+    lam0, _, conv0, it0, st0 = solve(pkg, d, e, Q=None)
+    lam1, V, conv1, it1, _ = solve(pkg, d, e)
+    assert conv0 and conv1 and it0 == it1 and st0["bulge_batches"] > 0
+    assert np.array_equal(lam0, lam1)           # the chase does not depend on Q
+    rng = np.random.default_rng(4)
+    Q0 = np.asfortranarray(rng.standard_normal((m, n)))
+    lam2, Q2, conv2, it2, _ = solve(pkg, d, e, Q=Q0.copy(order="F"))
+    assert np.array_equal(lam2, lam1)
+    err = np.linalg.norm(Q2 - Q0 @ V) / np.linalg.norm(Q0)
+    assert err <= 10 * n * EPS, err
+
+
+def test_multishift_fp32_q_and_device_tensors(cuda, pkg):
+    import torch
+    n = 1024
+    d, e = tridiag("C", n, seed=8)
+    dev = torch.device("cuda", 0)
+    td, te = torch.from_numpy(d.copy()).to(dev), torch.from_numpy(e.copy()).to(dev)
+    Q = torch.eye(n, dtype=torch.float32, device=dev).T
+    H = pkg.SymTridiagonal(td, te)
+    _, conv, it = pkg.qr_algorithm_(H, Q, chase_mode=3)
+    torch.cuda.synchronize()
+    assert conv
+    lam = td.cpu().numpy()
+    Q64 = Q.cpu().numpy().astype(np.float64)
+    eig, _, _ = errors(d, e, lam, None)
+    assert eig <= 1.0
+    # FP32 Q: residual and orthogonality at the FP32 level
+    eps32 = float(np.finfo(np.float32).eps)
+    TQ = d[:, None] * Q64
+    TQ[:-1] += e[:, None] * Q64[1:]
+    TQ[1:] += e[:, None] * Q64[:-1]
+    res = np.linalg.norm(TQ - Q64 * lam[None, :]) / np.sqrt(float((d * d).sum() + 2 * (e * e).sum()))
+    orth = np.linalg.norm(Q64.T @ Q64 - np.eye(n))
+    assert res <= 10 * n * eps32 and orth <= 10 * n * eps32, (res, orth)
+
+
+def test_multishift_maxiter(cuda, pkg):
+    """A batch never takes the sweep count past maxiter + 1, as single sweeps would not."""
+    n = 1000
+    d, e = tridiag("A", n, seed=2)
+    lam, Q, conv, it, st = solve(pkg, d, e, Q=None, maxiter=10)
+    assert not conv
+    assert it <= 11
