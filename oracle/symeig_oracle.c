@@ -130,27 +130,42 @@ static inline void rot_f32(float* x, float* y, float c, float s)
  *                        d[r] = c d[r],  d[r+1] = c d[r+1]
  *   form 2 (|s| >  |c|): k = c/s,  A = k (d[r]/d[r+1]),  B = -(k (d[r+1]/d[r])),
  *                        d[r] = s d[r+1],  d[r+1] = -(s d[r])
- * (every operation rounded once, divisions correctly rounded), and on every row
+ * and on every row
  *   (u, v) = form 2 ? (y, x) : (x, y);   x = fma(A, v, u);   y = fma(B, u, v).
- * Layers beyond the grid's (`layers`) are padding with A = B = +0, form 1 (the kernel's
- * zeroed table slots).  At the end of the pass column c is multiplied by d[c].  place (may
- * be NULL): layer L of rotation i is (1, 0) unless L < place[i], as for the canonical apply. */
-static void scaled_coeffs(double c, double s, double dr, double dr1, double* A, double* B, int* f2,
-                          double* nr, double* nr1)
+ * Every d is an unevaluated sum hi + lo, updated by dd_mul (an exact product to about
+ * 2^-106); A and B take the hi parts, each operation rounded once (divisions correctly
+ * rounded).  Layers beyond the grid's (`layers`) are padding with A = B = +0, form 1 (the
+ * kernel's zeroed table slots).  At the end of the pass column c is multiplied by the hi part
+ * of d[c].  place (may be NULL): layer L of rotation i is (1, 0) unless L < place[i], as for
+ * the canonical apply. */
+typedef struct { double hi, lo; } dd_t;
+
+static dd_t dd_mul(dd_t a, double m)
+{
+    const double p = a.hi * m;
+    double e = fma(a.hi, m, -p);
+    e = fma(a.lo, m, e);
+    const double h = p + e;
+    dd_t r = {h, e - (h - p)};
+    return r;
+}
+
+static void scaled_coeffs(double c, double s, dd_t dr, dd_t dr1, double* A, double* B, int* f2,
+                          dd_t* nr, dd_t* nr1)
 {
     if (fabs(s) > fabs(c)) {
         const double k = c / s;
-        *A = k * (dr / dr1);
-        *B = -(k * (dr1 / dr));
-        *nr = s * dr1;
-        *nr1 = -(s * dr);
+        *A = k * (dr.hi / dr1.hi);
+        *B = -(k * (dr1.hi / dr.hi));
+        *nr = dd_mul(dr1, s);
+        *nr1 = dd_mul(dr, -s);
         *f2 = 1;
     } else {
         const double k = s / c;
-        *A = k * (dr1 / dr);
-        *B = -(k * (dr / dr1));
-        *nr = c * dr;
-        *nr1 = c * dr1;
+        *A = k * (dr1.hi / dr.hi);
+        *B = -(k * (dr.hi / dr1.hi));
+        *nr = dd_mul(dr, c);
+        *nr1 = dd_mul(dr1, c);
         *f2 = 0;
     }
 }
@@ -160,9 +175,9 @@ int oracle_apply_scaled_pass_f64(double* Q, int64_t ldq, int64_t m, const double
                                  int64_t layers)
 {
     if (nloc < 2 || m <= 0) return 0;
-    double* d = (double*)malloc(sizeof(double) * nloc);
+    dd_t* d = (dd_t*)malloc(sizeof(dd_t) * nloc);
     if (!d) return -2;
-    for (int64_t c = 0; c < nloc; ++c) d[c] = 1.0;
+    for (int64_t c = 0; c < nloc; ++c) { d[c].hi = 1.0; d[c].lo = 0.0; }
     for (int64_t L = 0; L < 64; ++L)
         for (int64_t r = 0; r + 1 < nloc; ++r) {
             double A = 0.0, B = 0.0;
@@ -174,7 +189,7 @@ int oracle_apply_scaled_pass_f64(double* Q, int64_t ldq, int64_t m, const double
                     c = grid[2 * (i + LL * grid_rows)];
                     s = grid[2 * (i + LL * grid_rows) + 1];
                 }
-                double nr, nr1;
+                dd_t nr, nr1;
                 scaled_coeffs(c, s, d[r], d[r + 1], &A, &B, &f2, &nr, &nr1);
                 d[r] = nr;
                 d[r + 1] = nr1;
@@ -190,7 +205,7 @@ int oracle_apply_scaled_pass_f64(double* Q, int64_t ldq, int64_t m, const double
         }
     for (int64_t c = 0; c < nloc; ++c) {
         double* x = Q + (c0 + c) * ldq;
-        for (int64_t row = 0; row < m; ++row) x[row] = d[c] * x[row];
+        for (int64_t row = 0; row < m; ++row) x[row] = d[c].hi * x[row];
     }
     free(d);
     return 0;

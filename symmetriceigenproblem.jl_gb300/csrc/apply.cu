@@ -75,12 +75,18 @@ build_table_kernel(unsigned char* __restrict__ table, int64_t n_chunks,
 //                        d[r] <- s d[r+1],  d[r+1] <- -(s d[r]),
 // each operation rounded once (divisions correctly rounded), and column c is multiplied by
 // its final d[c] when it is stored.  |A B| <= 1 and every d loses at most a factor sqrt(2) per
-// rotation, so 64 layers keep d within [2^-64, 1]; the error per rotation is of the order of
-// the canonical form's (a few ulps).  Two kernels build the table:
+// rotation, so 64 layers keep d within [2^-64, 1].  The recurrence carries each d as an
+// unevaluated sum hi + lo (the products d <- m d exact to about 2^-106: p = RN(hi m),
+// e = fma(hi, m, -p), e = fma(lo, m, e), hi' = RN(p + e), lo' = RN(e - RN(hi' - p)))
+// and A, B and the final scale use hi.  With d rounded to one double at every product, the
+// rounding errors of a column's scale are shared by all rows of Q (unlike the per-element
+// errors of the canonical form) and add up pass after pass: ||Q^T Q - I|| of a full solve
+// grew to 2.3x the canonical form's at n = 4096 and 13x at n = 16384.  With hi + lo it equals
+// the canonical form's (0.0698 of 10 n eps at n = 4096, both).  Two kernels build the table:
 //   scaled_recurrence_kernel: the d recurrence itself.  Only the multiplications d <- c d
 //     form the chain; it runs as a wavefront (rotations r + 2L = step are independent and
 //     touch disjoint columns) on one CTA of one thread per layer, and records each
-//     rotation's d[r], d[r+1] before it, its form, and each column's final d.
+//     rotation's d[r], d[r+1] before it (hi), its form, and each column's final d (hi).
 //   scaled_table_kernel: A and B of every slot from those (the divisions, all independent),
 //     the group's flag word and, for group G-1, the final d of the column it stores.
 
@@ -92,8 +98,18 @@ constexpr int kPL = 2 * 63 + kRB;  // columns whose place[] a staging block need
 struct RecSmem {
     double2 cs[2][64][kRB + 1];   // rows padded by one pair: thread L reads row L
     int32_t pl[2][kPL + 2];
-    double d[256];
+    double2 d[256];  // (hi, lo) of the column scales
 };
+
+// (hi, lo) * m, about 2^-106 relative: the recurrence's scale update
+__device__ __forceinline__ double2 dd_mul(double2 a, double m)
+{
+    const double p = __dmul_rn(a.x, m);
+    double e = __fma_rn(a.x, m, -p);
+    e = __fma_rn(a.y, m, e);
+    const double h = __dadd_rn(p, e);
+    return make_double2(h, __dsub_rn(e, __dsub_rn(h, p)));
+}
 
 template <typename Tsrc>
 __device__ __forceinline__ double2 grid_cs(const Tsrc* grid, int64_t grid_rows, const int32_t* place,
@@ -154,7 +170,7 @@ scaled_recurrence_kernel(const double* __restrict__ grid, int64_t grid_rows,
     const int64_t last = nr - 1 + 2 * (layers - 1);     // last step
     const int64_t nblk = last / kRB + 1;
     const bool active = L < layers;
-    if (threadIdx.x == 0) sm.d[0] = 1.0;
+    if (threadIdx.x == 0) sm.d[0] = make_double2(1.0, 0.0);
     rec_stage(sm, 0, 0, grid, grid_rows, place, c0, nr, L0, layers);
     for (int64_t blk = 0; blk < nblk; ++blk) {
         const int buf = (int)(blk & 1);
@@ -170,33 +186,33 @@ scaled_recurrence_kernel(const double* __restrict__ grid, int64_t grid_rows,
             const int64_t t = T + k;
             if (t > last) break;   // uniform
             // column t+1 is first touched at step t (rotation (t, 0), thread 0)
-            if (threadIdx.x == 0 && t + 1 < n_loc) sm.d[(t + 1) & 255] = 1.0;
+            if (threadIdx.x == 0 && t + 1 < n_loc) sm.d[(t + 1) & 255] = make_double2(1.0, 0.0);
             const int64_t r = t - 2 * L;
             if (active && r >= 0 && r < nr) {
                 double2 cs = sm.cs[buf][L][k];
                 if (place != nullptr && L0 + L >= (int64_t)sm.pl[buf][r - (T - 126)]) cs = make_double2(1.0, 0.0);
                 const double c = cs.x, s = cs.y;
-                const double dr = sm.d[r & 255], dr1 = sm.d[(r + 1) & 255];
+                const double2 dr = sm.d[r & 255], dr1 = sm.d[(r + 1) & 255];
                 // |s| > |c| on the integer pipe (an FP64 compare costs an FP64 issue slot)
                 const uint64_t ac = (uint64_t)__double_as_longlong(c) & 0x7FFFFFFFFFFFFFFFull;
                 const uint64_t as = (uint64_t)__double_as_longlong(s) & 0x7FFFFFFFFFFFFFFFull;
                 const bool f2 = as > ac;
-                pre[L * nr + r] = make_double2(dr, dr1);
+                pre[L * nr + r] = make_double2(dr.x, dr1.x);
                 form[L * nr + r] = f2 ? 1 : 0;
                 // form 1: (c dr, c dr1); form 2: (s dr1, -(s dr)) = (s dr1, (-s) dr)
                 const double ns = __longlong_as_double(__double_as_longlong(s) ^ (long long)0x8000000000000000ull);
                 const double m1 = f2 ? s : c, m2 = f2 ? ns : c;
-                const double x1 = f2 ? dr1 : dr, x2 = f2 ? dr : dr1;
-                sm.d[r & 255] = m1 * x1;
-                sm.d[(r + 1) & 255] = m2 * x2;
+                const double2 x1 = f2 ? dr1 : dr, x2 = f2 ? dr : dr1;
+                sm.d[r & 255] = dd_mul(x1, m1);
+                sm.d[(r + 1) & 255] = dd_mul(x2, m2);
             }
             __syncthreads();
             // column t - 2 (layers - 1) had its last rotation at this step (and the last
             // column with it)
             const int64_t cf = t - 2 * (layers - 1);
             if (threadIdx.x == 0 && cf >= 0 && cf < nr) {
-                dfinal[cf] = sm.d[cf & 255];
-                if (cf == nr - 1) dfinal[cf + 1] = sm.d[(cf + 1) & 255];
+                dfinal[cf] = sm.d[cf & 255].x;
+                if (cf == nr - 1) dfinal[cf + 1] = sm.d[(cf + 1) & 255].x;
             }
         }
         __syncthreads();   // the staging buffer of this block is refilled next
