@@ -61,6 +61,9 @@ def parse_args():
     p.add_argument("--chase-mode", type=int, choices=[0, 1, 2, 3], default=0,
                    help="solve workload: 0 Newton-form two-warp chase, 1 reference form, 2 Newton + redo, "
                         "3 multishift batches")
+    p.add_argument("--ms-bulges", type=int, default=64, help="solve workload, chase mode 3: bulge cap of a batch")
+    p.add_argument("--ms-rows", type=int, default=16, help="solve workload, chase mode 3: block rows per bulge")
+    p.add_argument("--ms-release", type=int, default=4, help="solve workload, chase mode 3: steps between progress releases")
     p.add_argument("--count", type=int, default=4096, help="batched workload: number of tridiagonals")
     p.add_argument("--loop-sample", type=int, default=16,
                    help="batched workload: matrices timed one launch per matrix (extrapolated by sum n^2)")
@@ -474,6 +477,7 @@ def run_solve(args):
     dev = torch.device("cuda", 0)
     qdt = torch.float64 if args.q == "f64" else torch.float32
     h = pkg.Handle(0)
+    h.set_multishift(args.ms_bulges, args.ms_rows, args.ms_release)
     td, te = torch.from_numpy(d.copy()).to(dev), torch.from_numpy(e.copy()).to(dev)
     Q = torch.eye(n, dtype=qdt, device=dev).T
     torch.cuda.synchronize()
@@ -507,7 +511,9 @@ def run_solve(args):
         "dtype": "f64" if args.q == "f64" else "f64 chase, f32 Q",
         "data": "synthetic (seeded, as in the full-eigensolve configuration)",
         "config": {"workload": "qr_algorithm!(SymTridiagonal(d, e), Q = I)", "n": n, "case": args.case,
-                   "q": args.q, "max_layers": 128, "chase_mode": args.chase_mode, "form": args.form},
+                   "q": args.q, "max_layers": 128, "chase_mode": args.chase_mode, "form": args.form,
+                   **({"ms_bulges": args.ms_bulges, "ms_rows": args.ms_rows, "ms_release": args.ms_release}
+                      if args.chase_mode == 3 else {})},
         "converged": bool(conv), "iterations": it, "rotations": st["rotations"], "flushes": st["flushes"],
         "chase_ms": round(st["chase_ms"], 1), "apply_ms": round(st["apply_ms"], 1),
         "chase_us_per_rotation": round(st["chase_ms"] * 1e3 / max(st["rotations"], 1), 4),

@@ -79,16 +79,23 @@ int symeig_set_exact_order(symeig_handle h, int32_t exact_order);
  *   in the reference form (counted in redone_sweeps).
  * 1: the reference form (correctly rounded division and square root) on one thread.
  * 2: as 0, but every sweep is then redone in the reference form (exercises the restore).
- * 3: multishift.  Where a block has at least 2 * 64 rows and room for several layers, the
- *   chase runs a batch of up to 32 sweeps whose shifts are the eigenvalues of the block's
- *   trailing square (one per sweep), as bulges chased concurrently on separate SMs, each a
- *   fixed number of rows behind the one before.  The deflation test, the capacity rule and
+ * 3: multishift.  Where a block has at least 2 * 16 rows and room for several layers, the
+ *   chase runs a batch of up to 64 sweeps (symeig_set_multishift) whose shifts are the
+ *   eigenvalues of the block's trailing square (one per sweep), as bulges chased
+ *   concurrently on separate SMs, each a fixed number of rows behind the one before.  The deflation test, the capacity rule and
  *   the rotation placement are those of a sequence of single sweeps with those shifts; shorter
  *   blocks take the Wilkinson single sweep of mode 0.  Results meet the same error bounds as
  *   the reference (eigenvalues within 10 n eps ||T||, residual and orthogonality within
  *   10 n eps) but are not the reference's bits; the sweep count is higher (about 1.2-1.6x),
  *   the chase time far lower.  No reference counterpart. */
 int symeig_set_chase_mode(symeig_handle h, int32_t mode);
+/* Batch shape of chase mode 3: a batch over a block of len rows runs
+ * min(max_bulges, len / rows_per_bulge) bulges (and only when that is at least 2), and each
+ * bulge releases its progress to the next every release_every steps.  max_bulges in
+ * [2, 64] (default 64), rows_per_bulge >= 4 (default 16), release_every a power of two in
+ * [1, 64] (default 4).  No reference counterpart. */
+int symeig_set_multishift(symeig_handle h, int32_t max_bulges, int32_t rows_per_bulge,
+                          int32_t release_every);
 /* Arithmetic form of the FP64 bulk apply (symeig_apply_givens_f64*, and the qr driver's
  * apply with FP64 Q).  0 (default): every rotation as the reference's rmul!, four FP64
  * operations per rotation and row.  1: the scaled ("fast Givens") form: columns carry scale

@@ -33,6 +33,7 @@ SIGNATURES = {
     "symeig_get_stats": (ctypes.c_int, [c_vp, c_vp]),
     "symeig_set_exact_order": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_chase_mode": (ctypes.c_int, [c_vp, c_i32]),
+    "symeig_set_multishift": (ctypes.c_int, [c_vp, c_i32, c_i32, c_i32]),
     "symeig_set_apply_form": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_test_stall": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_get_rotation_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
@@ -161,6 +162,11 @@ class Handle:
     def set_apply_form(self, form):
         """0: canonical rotations (default); 1: the scaled form for FP64 applies."""
         check("symeig_set_apply_form", self._lib.symeig_set_apply_form(self.ptr, int(form)))
+
+    def set_multishift(self, max_bulges: int = 64, rows_per_bulge: int = 16, release_every: int = 4):
+        """Batch shape of chase mode 3 (symeig_set_multishift)."""
+        check("symeig_set_multishift", self._lib.symeig_set_multishift(
+            self.ptr, int(max_bulges), int(rows_per_bulge), int(release_every)))
 
     def set_chase_mode(self, mode):
         """0: Newton-form two-warp chase (default); 1: reference form; 2: Newton form with

@@ -61,6 +61,9 @@ struct symeig_context {
     int32_t chase_mode = 0;   // symeig_set_chase_mode
     int32_t apply_form = 0;   // symeig_set_apply_form
     int32_t test_stall = 0;   // symeig_set_test_stall
+    int32_t ms_bulges = kDefaultBulges;      // symeig_set_multishift
+    int32_t ms_rows = kDefaultRowsPerBulge;
+    int32_t ms_prog_every = kDefaultProgEvery;
     ChaseState* h_state = nullptr;  // pinned
     std::vector<cudaEvent_t> timing;  // pool of timing events
     symeig_stats stats{};
@@ -218,6 +221,9 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     init.status = CHASE_RUNNING;
     init.neg_zero = -0.0;
     init.chase_mode = h->chase_mode;
+    init.ms_bulges = h->ms_bulges;
+    init.ms_rows = h->ms_rows;
+    init.ms_prog_mask = h->ms_prog_every - 1;
     ChaseState* dstate = (ChaseState*)h->state.ptr;
 
     cudaStream_t ms = h->stream, cs = h->chase_stream;
@@ -248,18 +254,21 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
         CK(cudaEventRecord(c0, cs));
         BulgeScratch* bsc = (BulgeScratch*)h->bulge.ptr;
         CK(launch_chase(dstate, d, e, (double*)h->grid[b].ptr, (int32_t*)h->thick[b].ptr,
-                        (int32_t*)h->place[b].ptr, (double*)h->bak.ptr, bsc, cs));
+                        (int32_t*)h->place[b].ptr, (double*)h->bak.ptr, bsc, 0, cs));
         CK(cudaEventRecord(c1, cs));
         CK(cudaMemcpyAsync(h->h_state, dstate, sizeof(ChaseState), cudaMemcpyDeviceToHost, cs));
         CK(cudaEventRecord(h->ev_chased[b], cs));
         CK(cudaEventSynchronize(h->ev_chased[b]));
         // chase_mode 3: each multishift batch runs in its own cooperative launch, after which
-        // the chase kernel resumes the flush
+        // the chase kernel resumes the flush.  kBatchesAhead (batch, resume) pairs are queued
+        // per host round trip; those queued after the flush's last batch return at once.
         while (h->h_state->status == CHASE_BATCH) {
-            CK(launch_bulge_batch(dstate, d, e, (double*)h->grid[b].ptr, (const int32_t*)h->thick[b].ptr,
-                                  bsc, h->derr, h->h_state->b_bulges, cs));
-            CK(launch_chase(dstate, d, e, (double*)h->grid[b].ptr, (int32_t*)h->thick[b].ptr,
-                            (int32_t*)h->place[b].ptr, (double*)h->bak.ptr, bsc, cs));
+            for (int k = 0; k < kBatchesAhead; ++k) {
+                CK(launch_bulge_batch(dstate, d, e, (double*)h->grid[b].ptr,
+                                      (const int32_t*)h->thick[b].ptr, bsc, h->derr, h->ms_bulges, cs));
+                CK(launch_chase(dstate, d, e, (double*)h->grid[b].ptr, (int32_t*)h->thick[b].ptr,
+                                (int32_t*)h->place[b].ptr, (double*)h->bak.ptr, bsc, 1, cs));
+            }
             CK(cudaEventRecord(c1, cs));
             CK(cudaMemcpyAsync(h->h_state, dstate, sizeof(ChaseState), cudaMemcpyDeviceToHost, cs));
             CK(cudaEventRecord(h->ev_chased[b], cs));
@@ -600,6 +609,18 @@ int symeig_set_chase_mode(symeig_handle h, int32_t mode)
     if (!h) return SYMEIG_ERR_HANDLE;
     if (mode < 0 || mode > 3) return SYMEIG_ERR_SIZE;
     h->chase_mode = mode;
+    return SYMEIG_OK;
+}
+
+int symeig_set_multishift(symeig_handle h, int32_t max_bulges, int32_t rows_per_bulge,
+                          int32_t release_every)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    if (max_bulges < 2 || max_bulges > kMaxBulges || rows_per_bulge < 4) return SYMEIG_ERR_SIZE;
+    if (release_every < 1 || release_every > 64 || (release_every & (release_every - 1))) return SYMEIG_ERR_SIZE;
+    h->ms_bulges = max_bulges;
+    h->ms_rows = rows_per_bulge;
+    h->ms_prog_every = release_every;
     return SYMEIG_OK;
 }
 

@@ -288,48 +288,66 @@ __device__ __forceinline__ int32_t warp_max(int32_t v)
 
 // ---- multishift batches (chase_mode 3) -----------------------------------------------------
 //
-// Shifts of a batch of nb bulges over a block ending at row `to` (1-based): the eigenvalues of
-// the block's trailing nb x nb principal submatrix, ascending.  The submatrix is scaled by an
-// exact power of two to max |entry| in [0.5, 1); lane l < nb brackets the l-th eigenvalue by
-// bisection on FP32 Sturm counts, then takes up to three FP64 Newton steps on the
-// characteristic polynomial (three-term recurrence for p and p').  A step that is not finite
-// or leaves the FP32 bracket's neighbourhood is refused (clustered roots).  FP32 shifts alone
-// cost about 25 % more sweeps: the bulges' reduction of the trailing couplings is limited by
-// the shifts' distance to the eigenvalues.  All 32 lanes of warp 0 call it; sd, se2 and sea
-// (FP32) and dd, ee2 (FP64) are 32-entry shared arrays.
+// Shifts of a batch of nb <= kMaxBulges = 64 bulges over a block ending at row `to` (1-based):
+// the eigenvalues of the block's trailing nb x nb principal submatrix, ascending.  The
+// submatrix is scaled by an exact power of two to max |entry| in [0.5, 1); each eigenvalue
+// is bracketed by bisection on FP32 Sturm counts, then takes up to three FP64 Newton steps on
+// the characteristic polynomial (three-term recurrence for p and p').  A step that is not
+// finite or leaves the FP32 bracket's neighbourhood is refused (clustered roots).  FP32 shifts
+// alone cost about 25 % more sweeps: the bulges' reduction of the trailing couplings is
+// limited by the shifts' distance to the eigenvalues.  All 32 lanes of warp 0 call it; lane l
+// finds eigenvalues l and l + 32; sd, se2, sea (FP32) and dd, ee2 (FP64) are
+// kMaxBulges-entry shared arrays.
 __device__ void batch_shifts(const double* __restrict__ dv, const double* __restrict__ ev,
                              int64_t to, int nb, double* __restrict__ shifts, float* sd, float* se2,
                              float* sea, double* dd, double* ee2)
 {
     const int lane = threadIdx.x & 31;
     const int64_t r0 = to - nb;  // 0-based first row of the submatrix
-    const double dq = lane < nb ? dv[r0 + lane] : 0.0;
-    const double eq = lane < nb - 1 ? ev[r0 + lane] : 0.0;
-    double mx = fmax(fabs(dq), fabs(eq));
+    // lane holds entries q = lane and lane + 32 of the submatrix
+    double dq[2], eq[2];
+    double mx = 0.0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int q = lane + 32 * h;
+        dq[h] = q < nb ? dv[r0 + q] : 0.0;
+        eq[h] = q < nb - 1 ? ev[r0 + q] : 0.0;
+        mx = fmax(mx, fmax(fabs(dq[h]), fabs(eq[h])));
+    }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (!(mx > 0.0) || !isfinite(mx)) {
         // a zero block is already diagonal; a non-finite one is left to the sweep
-        if (lane < nb) shifts[lane] = dq;
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (lane + 32 * h < nb) shifts[lane + 32 * h] = dq[h];
         __syncwarp();
         return;
     }
     int ex;
     frexp(mx, &ex);
-    const double dsc = ldexp(dq, -ex), esc = ldexp(eq, -ex);
-    const float df = (float)dsc, ef = (float)esc;
-    sd[lane] = df;
-    se2[lane] = ef * ef;
-    sea[lane] = fabsf(ef);
-    dd[lane] = dsc;
-    ee2[lane] = esc * esc;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int q = lane + 32 * h;
+        const double dsc = ldexp(dq[h], -ex), esc = ldexp(eq[h], -ex);
+        const float ef = (float)esc;
+        sd[q] = (float)dsc;
+        se2[q] = ef * ef;
+        sea[q] = fabsf(ef);
+        dd[q] = dsc;
+        ee2[q] = esc * esc;
+    }
     __syncwarp();
     // Gershgorin interval of the submatrix
     float lo = 3.0f, hi = -3.0f;
-    if (lane < nb) {
-        const float rad = (lane >= 1 ? sea[lane - 1] : 0.0f) + (lane < nb - 1 ? sea[lane] : 0.0f);
-        lo = df - rad;
-        hi = df + rad;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int q = lane + 32 * h;
+        if (q < nb) {
+            const float rad = (q >= 1 ? sea[q - 1] : 0.0f) + (q < nb - 1 ? sea[q] : 0.0f);
+            lo = fminf(lo, sd[q] - rad);
+            hi = fmaxf(hi, sd[q] + rad);
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -339,38 +357,43 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
     lo -= 1e-6f;
     hi += 1e-6f;
     constexpr float kPiv = 1e-30f;
-    for (int it = 0; it < 40; ++it) {
-        const float mid = 0.5f * (lo + hi);
-        if (!(mid > lo && mid < hi)) break;
-        // number of eigenvalues below mid (negative pivots of T - mid I = L D L^T)
-        float q = sd[0] - mid;
-        int cnt = q < 0.0f;
-        for (int i = 1; i < nb; ++i) {
-            if (fabsf(q) < kPiv) q = -kPiv;
-            q = (sd[i] - mid) - se2[i - 1] / q;
-            cnt += q < 0.0f;
+    for (int h = 0; h < 2; ++h) {
+        const int k = lane + 32 * h;   // the eigenvalue this lane finds
+        if (32 * h >= nb) break;       // uniform
+        float a = lo, b = hi;
+        for (int it = 0; it < 40; ++it) {
+            const float mid = 0.5f * (a + b);
+            if (!(mid > a && mid < b)) break;
+            // number of eigenvalues below mid (negative pivots of T - mid I = L D L^T)
+            float q = sd[0] - mid;
+            int cnt = q < 0.0f;
+            for (int i = 1; i < nb; ++i) {
+                if (fabsf(q) < kPiv) q = -kPiv;
+                q = (sd[i] - mid) - se2[i - 1] / q;
+                cnt += q < 0.0f;
+            }
+            if (cnt > k) b = mid;
+            else a = mid;
         }
-        if (cnt > lane) hi = mid;
-        else lo = mid;
-    }
-    double x = (double)(0.5f * (lo + hi));
-    for (int it = 0; it < 3; ++it) {
-        double p0 = 1.0, p1 = dd[0] - x, q0 = 0.0, q1 = -1.0;
-        for (int i = 1; i < nb; ++i) {
-            const double a = dd[i] - x, b = ee2[i - 1];
-            const double p2 = a * p1 - b * p0;
-            const double q2 = a * q1 - p1 - b * q0;
-            p0 = p1;
-            p1 = p2;
-            q0 = q1;
-            q1 = q2;
+        double x = (double)(0.5f * (a + b));
+        for (int it = 0; it < 3; ++it) {
+            double p0 = 1.0, p1 = dd[0] - x, q0 = 0.0, q1 = -1.0;
+            for (int i = 1; i < nb; ++i) {
+                const double aa = dd[i] - x, bb = ee2[i - 1];
+                const double p2 = aa * p1 - bb * p0;
+                const double q2 = aa * q1 - p1 - bb * q0;
+                p0 = p1;
+                p1 = p2;
+                q0 = q1;
+                q1 = q2;
+            }
+            const double step = p1 / q1;
+            if (!isfinite(step) || fabs(step) > 1e-5) break;
+            x -= step;
+            if (fabs(step) <= 1e-17 * fabs(x)) break;
         }
-        const double step = p1 / q1;
-        if (!isfinite(step) || fabs(step) > 1e-5) break;
-        x -= step;
-        if (fabs(step) <= 1e-17 * fabs(x)) break;
+        if (k < nb) shifts[k] = ldexp(x, ex);
     }
-    if (lane < nb) shifts[lane] = ldexp(x, ex);
     __syncwarp();
 }
 
@@ -379,7 +402,7 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
 // bulge's stores: step k of a sweep stores dv[k-1] and ev[k-2] (0-based; its last step also
 // dv[k] and ev[k-1]), so before its loads for step i+1 (dv[i+1], ev[i+1]) bulge j needs bulge
 // j-1 through step min(i+3, to-1).  The helper warp's store thread releases the bulge's
-// progress every kProgEvery steps and at its last step (st.release.gpu); the next bulge's
+// progress every (prog_mask + 1) steps and at its last step (st.release.gpu); the next bulge's
 // warps read it with ld.acquire.gpu only when the value they hold is too small, and read
 // dv/ev through L2 (ld.global.cg), never from a stale L1 line.  Bulge j waits only for bulge
 // j-1 and the CTAs are co-resident (one cooperative launch), so the waits form one chain that
@@ -388,7 +411,6 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
 // two warps' barrier protocol still completes; the call then reports the error.
 // The rotation is givens_nr_core (reference form out of its range) without the rounding
 // proof: the batch is not the reference's sweep sequence, so there are no bits to match.
-constexpr int kProgEvery = 8;
 
 __device__ __forceinline__ long long ld_acquire_gpu(const long long* p)
 {
@@ -435,7 +457,7 @@ __device__ void sweep_bulge_2w(double* __restrict__ dv, double* __restrict__ ev,
                                int64_t to, double mu, double* __restrict__ grid,
                                const int32_t* __restrict__ thick, int64_t rows, int32_t layer,
                                int32_t jofs, double nz, NrMail* mail, PipeWait pw,
-                               long long* __restrict__ my_prog)
+                               long long* __restrict__ my_prog, int64_t prog_mask)
 {
     const int warp = threadIdx.x >> 5;
     const bool lead = (threadIdx.x & 31) == 0;
@@ -508,7 +530,7 @@ __device__ void sweep_bulge_2w(double* __restrict__ dv, double* __restrict__ ev,
                     dv[i] = B22pp;
                     ev[i - 1] = __fma_rn(B12p, c, -mulz(B11p, s, nz));
                 }
-                if (i == to - 1 || (i - from) % kProgEvery == kProgEvery - 1) st_release_gpu(my_prog, i);
+                if (i == to - 1 || ((i - from) & prog_mask) == prog_mask) st_release_gpu(my_prog, i);
             }
             B11 = B22pp;
             B21 = e_next;
@@ -528,6 +550,7 @@ bulge_batch_kernel(const ChaseState* __restrict__ st, double* __restrict__ dv,
 {
     __shared__ NrMail mail[2];
     const int j = blockIdx.x;
+    if (st->status != CHASE_BATCH) return;  // a launch queued ahead after the batches ended
     const int32_t nb = st->b_bulges;
     if (j >= nb) return;
     const int64_t n = st->n, from = st->b_from, to = st->b_to;
@@ -535,7 +558,7 @@ bulge_batch_kernel(const ChaseState* __restrict__ st, double* __restrict__ dv,
     const int32_t L0 = st->b_layer0;
     PipeWait pw{j > 0 ? &bs->prog[j - 1] : nullptr, err, -1};
     sweep_bulge_2w(dv, ev, from, to, bs->shifts[j], grid, thick, rows, L0 > 0 ? L0 + j : 0, j,
-                   st->neg_zero, mail, pw, &bs->prog[j]);
+                   st->neg_zero, mail, pw, &bs->prog[j], (int64_t)st->ms_prog_mask);
 }
 
 // One flush: the reference's inner loop from `to = last_block_ends_at` until the matrix is
@@ -563,13 +586,13 @@ struct Decision {
 __global__ void __launch_bounds__(64, 1)
 chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __restrict__ ev,
              double* __restrict__ grid, int32_t* __restrict__ thick, int32_t* __restrict__ place,
-             double* __restrict__ bak, BulgeScratch* __restrict__ bs)
+             double* __restrict__ bak, BulgeScratch* __restrict__ bs, int32_t resume_only)
 {
     __shared__ NrMail mail[2];
     __shared__ Decision dec;
     __shared__ int32_t fail;
-    __shared__ float ms_d[32], ms_e2[32], ms_ea[32];
-    __shared__ double ms_dd[32], ms_ee2[32];
+    __shared__ float ms_d[kMaxBulges], ms_e2[kMaxBulges], ms_ea[kMaxBulges];
+    __shared__ double ms_dd[kMaxBulges], ms_ee2[kMaxBulges];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int64_t n = st->n;
@@ -581,6 +604,8 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
     const bool exact = st->exact_order != 0;
     const int64_t maxiter = st->maxiter;
     const int32_t mode = st->chase_mode;
+    const int32_t ms_bulges = min(max(st->ms_bulges, 2), kMaxBulges);
+    const int64_t ms_rows = max(st->ms_rows, 4);
     int64_t iter = st->iter;
     int64_t lbe = st->last_block_ends_at;
     const int64_t rows = n > 1 ? n - 1 : 1;
@@ -591,6 +616,7 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
     // index of its block got one layer per bulge (bulge j at layer thick + 1 + j, or at the
     // exact-order layer b_layer0 + j).
     const bool resume = st->resume != 0;
+    if (resume_only && !resume) return;  // a launch queued ahead after the batches ended
     if (!resume) {
         for (int64_t q = threadIdx.x; q < n; q += 64) {
             thick[q] = 0;
@@ -672,7 +698,7 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
                             if (mode == 3) {
                                 int64_t cap = (int64_t)max_layers - mx;
                                 if (exact) cap = min(cap, (int64_t)grid_layers - layer + 1);
-                                nbl = min(min((int64_t)kMaxBulges, (to - from + 1) / kRowsPerBulge), cap);
+                                nbl = min(min((int64_t)ms_bulges, (to - from + 1) / ms_rows), cap);
                                 nbl = min(nbl, maxiter - iter + 1);
                             }
                             if (nbl >= 2) {
@@ -919,9 +945,10 @@ cudaError_t launch_get_rotation(int64_t count, const double* f, const double* g,
 }
 
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
-                         int32_t* place, double* bak, BulgeScratch* bs, cudaStream_t stream)
+                         int32_t* place, double* bak, BulgeScratch* bs, int32_t resume_only,
+                         cudaStream_t stream)
 {
-    chase_kernel<<<1, 64, 0, stream>>>(state, d, e, grid, thick, place, bak, bs);
+    chase_kernel<<<1, 64, 0, stream>>>(state, d, e, grid, thick, place, bak, bs, resume_only);
     return cudaGetLastError();
 }
 

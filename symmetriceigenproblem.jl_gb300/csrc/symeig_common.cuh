@@ -55,10 +55,16 @@ enum ChaseStatus : int32_t {
     CHASE_BATCH     = 4,   // a multishift batch is pending: run it, then resume the flush
 };
 
-// Multishift batches (chase_mode 3): at most kMaxBulges bulges per batch, and a batch over a
-// block of len rows has at most len / kRowsPerBulge bulges.
-constexpr int kMaxBulges = 32;
-constexpr int kRowsPerBulge = 64;
+// Multishift batches (chase_mode 3): a batch over a block of len rows has at most
+// min(ms_bulges, len / ms_rows) bulges (ChaseState; defaults kDefaultBulges and
+// kDefaultRowsPerBulge, the fastest measured at n = 2000 and 16384), and never more than
+// kMaxBulges.  A bulge releases its progress every kDefaultProgEvery steps; the host queues
+// kBatchesAhead batches per round trip.
+constexpr int kMaxBulges = 64;
+constexpr int kDefaultBulges = 64;
+constexpr int kDefaultRowsPerBulge = 16;
+constexpr int kDefaultProgEvery = 4;
+constexpr int kBatchesAhead = 8;
 
 // Device scratch of a batch: the bulges' shifts and their progress words.
 struct BulgeScratch {
@@ -97,6 +103,10 @@ struct ChaseState {
     int32_t r_did;
     int64_t r_to, r_rotations, r_min_from, r_max_to, r_early;
     int64_t batches;             // batches run (cumulative)
+    int32_t ms_bulges;           // bulge cap of a batch (2 .. kMaxBulges)
+    int32_t ms_rows;             // rows of a block per bulge (>= 4)
+    int32_t ms_prog_mask;        // a bulge releases its progress every (mask + 1) steps
+    int32_t pad1;
 };
 
 // ---- launch helpers (defined in the .cu files) ------------------------------------------
@@ -151,10 +161,13 @@ cudaError_t launch_tridiag_unscale(double* A, int64_t lda, int64_t n, double* d,
 // givensAlgorithm elementwise on device arrays (form 0 Newton form, 1 reference form).
 cudaError_t launch_get_rotation(int64_t count, const double* f, const double* g, double* c,
                                 double* s, double* r, int32_t form, cudaStream_t stream);
+// resume_only: run only if a multishift batch is pending resumption (else return at once).
 cudaError_t launch_chase(ChaseState* state, double* d, double* e, double* grid, int32_t* thick,
-                         int32_t* place, double* bak, BulgeScratch* bs, cudaStream_t stream);
-// The pending multishift batch of `state` (status CHASE_BATCH): `bulges` CTAs of two warps in
-// one cooperative launch, one bulge each.  A bounded wait that gives up sets *err.
+                         int32_t* place, double* bak, BulgeScratch* bs, int32_t resume_only,
+                         cudaStream_t stream);
+// The pending multishift batch of `state`, if its status is CHASE_BATCH (else the launch
+// returns at once): `bulges` (>= the batch's) CTAs of two warps in one cooperative launch,
+// one bulge each.  A bounded wait that gives up sets *err.
 cudaError_t launch_bulge_batch(const ChaseState* state, double* d, double* e, double* grid,
                                const int32_t* thick, BulgeScratch* bs, int* err, int32_t bulges,
                                cudaStream_t stream);

@@ -2,8 +2,8 @@
 eigenvalues of the block's trailing square, chased as concurrent bulges.  It is not the
 reference's sweep sequence, so it is checked against the error bounds the reference meets
 (eigenvalues within 10 n eps ||T|| of LAPACK, ||TQ - QD||_F / ||T||_F and ||Q^T Q - I||_F
-within 10 n eps), and, where no block is long enough for a batch (n < 128), against the
-oracle bit for bit."""
+within 10 n eps), and, where no block is long enough for a batch, against the oracle bit for
+bit."""
 from __future__ import annotations
 
 import numpy as np
@@ -35,12 +35,14 @@ def errors(d, e, lam, Q):
     return eig, res, orth
 
 
-def solve(pkg, d, e, Q="eye", **kw):
+def solve(pkg, d, e, Q="eye", ms=None, **kw):
     n = d.size
     H = pkg.SymTridiagonal(d.copy(), e.copy())
     if isinstance(Q, str):
         Q = np.asfortranarray(np.eye(n))
     h = pkg.Handle(0)
+    if ms is not None:
+        h.set_multishift(*ms)
     try:
         _, conv, it = pkg.qr_algorithm_(H, Q, handle=h, chase_mode=3, **kw)
         st = h.stats()
@@ -49,13 +51,15 @@ def solve(pkg, d, e, Q="eye", **kw):
     return H.dv, Q, conv, it, st
 
 
-@pytest.mark.parametrize("kind,n", [("C", 100), ("A", 127), ("split", 120), ("B", 64)])
-def test_multishift_short_blocks_are_the_reference(cuda, pkg, oracle, kind, n):
-    """No block below 2 x 64 rows takes a batch: mode 3 is then mode 0, the oracle's bits."""
+@pytest.mark.parametrize("kind,n,rows", [("C", 100, 64), ("A", 127, 64), ("split", 120, 64),
+                                         ("B", 64, 64), ("C", 31, 16), ("A", 20, 16)])
+def test_multishift_short_blocks_are_the_reference(cuda, pkg, oracle, kind, n, rows):
+    """No block below 2 x rows_per_bulge rows takes a batch: mode 3 is then mode 0, the
+    oracle's bits."""
     d, e = tridiag(kind, n, seed=n)
     od, oe, oQ = d.copy(), e.copy(), np.asfortranarray(np.eye(n))
     conv_o, it_o, _, _ = oracle.qr_algorithm(od, oe, oQ)
-    lam, Q, conv, it, st = solve(pkg, d, e)
+    lam, Q, conv, it, st = solve(pkg, d, e, ms=(64, rows, 8))
     assert st["bulge_batches"] == 0
     assert (conv, it) == (conv_o, it_o)
     assert np.array_equal(lam, od) and np.array_equal(Q, oQ)
@@ -140,6 +144,31 @@ def test_multishift_fp32_q_and_device_tensors(cuda, pkg):
     res = np.linalg.norm(TQ - Q64 * lam[None, :]) / np.sqrt(float((d * d).sum() + 2 * (e * e).sum()))
     orth = np.linalg.norm(Q64.T @ Q64 - np.eye(n))
     assert res <= 10 * n * eps32 and orth <= 10 * n * eps32, (res, orth)
+
+
+@pytest.mark.parametrize("kind,n", [("B", 1500), ("split", 900)])
+def test_multishift_pipelining_is_exact(cuda, pkg, kind, n):
+    """For given shifts the pipelined bulges compute what the same sweeps run one after
+    another compute: the result does not depend on how far apart the bulges run (a release
+    every 1, 8 or 64 steps) -- bit for bit, eigenvalues and Q."""
+    d, e = tridiag(kind, n, seed=n + 3)
+    runs = [solve(pkg, d, e, ms=(64, 16, r)) for r in (1, 8, 64)]
+    for lam, Q, conv, it, st in runs[1:]:
+        assert conv and it == runs[0][3] and st["bulge_batches"] == runs[0][4]["bulge_batches"]
+        assert np.array_equal(lam, runs[0][0]) and np.array_equal(Q, runs[0][1])
+    assert runs[0][4]["bulge_batches"] > 0
+
+
+def test_multishift_settings_are_checked(cuda, pkg):
+    h = pkg.Handle(0)
+    try:
+        for bad in ((1, 16, 8), (65, 16, 8), (64, 3, 8), (64, 16, 0), (64, 16, 3), (64, 16, 128)):
+            with pytest.raises(pkg.SymeigError):
+                h.set_multishift(*bad)
+        h.set_multishift(2, 4, 1)
+        h.set_multishift(64, 1 << 20, 64)
+    finally:
+        h.close()
 
 
 def test_multishift_maxiter(cuda, pkg):
