@@ -18,7 +18,8 @@ and three additions without a reference counterpart:
     bulk_wave_order_2x2_lmul!(A, givens)                      # bulk form of lmul!, src/simple_givens.jl:38
     get_rotation(f, g) -> (c, s, r), elementwise               # src/simple_givens.jl:20
     syev!(A) -> (lam, V): dense symmetric eigensolve (sytrd, orgtr, qr_algorithm!)
-    set_apply_form!(form), set_chase_mode!(mode): the library's arithmetic options
+    set_apply_form!(form), set_chase_mode!(mode), set_multishift!(bulges, rows, release):
+        the library's arithmetic options (chase mode 3 is the multishift chase)
 
 Q may be Matrix{Float64} or Matrix{Float32} (the FP32-Q variant: FP64 chase, (c,s) rounded to
 Float32).  Host arrays are copied to the GPU and back by the library.  Nothing is exported,
@@ -186,9 +187,18 @@ set_apply_form!(form::Integer) =
     check(:symeig_set_apply_form, ccall((:symeig_set_apply_form, libsymeig), Cint, (Ptr{Cvoid}, Int32), handle(), form))
 
 """0: Newton-form two-warp chase (default); 1: reference form; 2: Newton form with every
-sweep redone in the reference form.  All give the same bits."""
+sweep redone in the reference form -- these three give the reference's bits.  3: multishift
+batches of concurrent bulges (within the reference's error bounds, not its bits; about 8x
+faster at n = 16384)."""
 set_chase_mode!(mode::Integer) =
     check(:symeig_set_chase_mode, ccall((:symeig_set_chase_mode, libsymeig), Cint, (Ptr{Cvoid}, Int32), handle(), mode))
+
+"""Batch shape of chase mode 3: at most `bulges` (2..64, default 64) bulges per batch, one per
+`rows` (default 16) rows of the block, each releasing its progress every `release` steps
+(a power of two, default 4)."""
+set_multishift!(bulges::Integer = 64, rows::Integer = 16, release::Integer = 4) =
+    check(:symeig_set_multishift, ccall((:symeig_set_multishift, libsymeig), Cint,
+          (Ptr{Cvoid}, Int32, Int32, Int32), handle(), bulges, rows, release))
 
 function eigen_decomp!(H::SymTridiagonal{Float64})
     n = size(H, 1)
