@@ -18,6 +18,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <new>
+#include <type_traits>
 #include <vector>
 
 #include "symeig.h"
@@ -158,11 +159,21 @@ int apply_grid(symeig_handle h, T* Q, int64_t ldq, int64_t m, const Tsrc* grid, 
 {
     if (m <= 0 || n_loc < 2 || layers <= 0) return SYMEIG_OK;
     const int64_t per = apply_layers_per_pass<T>();
-    CK(h->table.ensure(apply_table_bytes<T>(n_loc, per)));
+    CK(h->table.ensure(apply_table_bytes<T>(n_loc, layers)));
+    // the scaled form: the column-scale recurrences of all passes at once
+    bool rec_all = false;
+    if constexpr (std::is_same<Tsrc, double>::value && std::is_same<T, double>::value) {
+        if (h->apply_form == 1 && layers > per) {
+            CK(launch_scaled_recurrences(grid, grid_rows, thick, c0, n_loc, 0, layers, h->table.ptr, s));
+            rec_all = true;
+        }
+    }
     for (int64_t L0 = 0; L0 < layers; L0 += per) {
         ApplyPass pass{c0, n_loc, L0, std::min(per, layers - L0), rs};
         pass.form = sizeof(T) == 8 ? h->apply_form : 0;
         pass.stall = h->test_stall;
+        pass.rec = rec_all ? 1 : 0;
+        pass.slot = rec_all ? (int32_t)(L0 / per) : 0;
         cudaEvent_t e0 = nullptr, e1 = nullptr;
         if (h->kernel_timing) {
             e0 = kernel_event(h);

@@ -157,14 +157,32 @@ __device__ __forceinline__ void rec_stage(RecSmem& sm, int buf, int64_t blk, con
 // The d recurrence of one pass (see the section comment); one CTA of 64 threads, thread L =
 // layer L of the pass; step t treats rotation (t - 2L, L).  The grid is FP64 (the scaled
 // form is FP64 only).
+__host__ __device__ inline size_t scaled_pre_bytes(int64_t n_loc) { return (size_t)64 * (size_t)(n_loc - 1) * 16; }
+__host__ __device__ inline size_t scaled_form_bytes(int64_t n_loc) { return ((size_t)64 * (size_t)(n_loc - 1) + 255) & ~(size_t)255; }
+// one pass's scratch slot: pre (64 x (n_loc-1) double2), form (64 x (n_loc-1) bytes, padded),
+// dfinal (n_loc doubles), padded to 256 bytes
+__host__ __device__ inline size_t scaled_slot_bytes(int64_t n_loc)
+{
+    return (scaled_pre_bytes(n_loc) + scaled_form_bytes(n_loc) + (size_t)n_loc * sizeof(double) + 255) &
+           ~(size_t)255;
+}
+
+// CTA b runs the recurrence of pass b of a flush: layers [L0 + 64 b, L0 + 64 b + 64) of the
+// layers_total from L0 on, into scratch slot b.  The passes' recurrences are independent (d
+// starts at 1 in every pass), so one launch of all of a flush's passes costs one pass.
 __global__ void __launch_bounds__(64)
 scaled_recurrence_kernel(const double* __restrict__ grid, int64_t grid_rows,
-                         const int32_t* __restrict__ place, int64_t c0, int64_t n_loc, int64_t L0,
-                         int64_t layers, double2* __restrict__ pre, unsigned char* __restrict__ form,
-                         double* __restrict__ dfinal)
+                         const int32_t* __restrict__ place, int64_t c0, int64_t n_loc, int64_t L0_all,
+                         int64_t layers_total, unsigned char* __restrict__ scratch, size_t slot_bytes)
 {
     extern __shared__ __align__(16) unsigned char rec_raw[];
     RecSmem& sm = *reinterpret_cast<RecSmem*>(rec_raw);
+    const int64_t L0 = L0_all + 64 * (int64_t)blockIdx.x;
+    const int64_t layers = layers_total - 64 * (int64_t)blockIdx.x < 64 ? layers_total - 64 * (int64_t)blockIdx.x : 64;
+    unsigned char* slot = scratch + (size_t)blockIdx.x * slot_bytes;
+    double2* __restrict__ pre = (double2*)slot;
+    unsigned char* __restrict__ form = slot + scaled_pre_bytes(n_loc);
+    double* __restrict__ dfinal = (double*)(form + scaled_form_bytes(n_loc));
     const int L = threadIdx.x;
     const int64_t nr = n_loc - 1;                       // rotations per layer
     const int64_t last = nr - 1 + 2 * (layers - 1);     // last step
@@ -297,18 +315,30 @@ template <typename T> size_t table_region(int64_t n_loc)
     return (b + 255) & ~(size_t)255;
 }
 
-// the scaled form's scratch after the table: pre (64 x (n_loc-1) double2), form (64 x
-// (n_loc-1) bytes, padded), dfinal (n_loc doubles)
-inline size_t scaled_pre_bytes(int64_t n_loc) { return (size_t)64 * (size_t)(n_loc - 1) * 16; }
-inline size_t scaled_form_bytes(int64_t n_loc) { return ((size_t)64 * (size_t)(n_loc - 1) + 255) & ~(size_t)255; }
-
+// FP64: the scaled form's scratch follows the table, one slot per pass of `layers`
 template <typename T> size_t apply_table_bytes(int64_t n_loc, int64_t layers)
 {
-    (void)layers;
     size_t b = table_region<T>(n_loc);
-    if (sizeof(T) == 8 && n_loc >= 2)
-        b += scaled_pre_bytes(n_loc) + scaled_form_bytes(n_loc) + (size_t)n_loc * sizeof(double);
+    if (sizeof(T) == 8 && n_loc >= 2) {
+        const int64_t passes = layers > 64 ? (layers + 63) / 64 : 1;
+        b += (size_t)passes * scaled_slot_bytes(n_loc);
+    }
     return b;
+}
+
+cudaError_t launch_scaled_recurrences(const double* grid, int64_t grid_rows, const int32_t* place,
+                                      int64_t c0, int64_t n_loc, int64_t L0, int64_t layers,
+                                      void* table, cudaStream_t stream)
+{
+    if (n_loc < 2 || layers <= 0) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(scaled_recurrence_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(RecSmem));
+    if (e != cudaSuccess) return e;
+    const unsigned passes = (unsigned)((layers + 63) / 64);
+    scaled_recurrence_kernel<<<passes, 64, sizeof(RecSmem), stream>>>(
+        grid, grid_rows, place, c0, n_loc, L0, layers,
+        (unsigned char*)table + table_region<double>(n_loc), scaled_slot_bytes(n_loc));
+    return cudaGetLastError();
 }
 template size_t apply_table_bytes<double>(int64_t, int64_t);
 template size_t apply_table_bytes<float>(int64_t, int64_t);
@@ -330,15 +360,19 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
     if constexpr (sizeof(T) == 8) {
         if (pass.form == 1) {
             unsigned char* tb = (unsigned char*)table;
-            double2* pre = (double2*)(tb + table_region<T>(pass.n_loc));
-            unsigned char* form = (unsigned char*)pre + scaled_pre_bytes(pass.n_loc);
+            unsigned char* slot = tb + table_region<T>(pass.n_loc) + (size_t)pass.slot * scaled_slot_bytes(pass.n_loc);
+            double2* pre = (double2*)slot;
+            unsigned char* form = slot + scaled_pre_bytes(pass.n_loc);
             double* dfinal = (double*)(form + scaled_form_bytes(pass.n_loc));
             static_assert(sizeof(Tsrc) == 8, "the scaled form reads an FP64 grid");
-            e = cudaFuncSetAttribute(scaled_recurrence_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)sizeof(RecSmem));
-            if (e != cudaSuccess) return e;
-            scaled_recurrence_kernel<<<1, 64, sizeof(RecSmem), stream>>>(
-                (const double*)grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers, pre, form, dfinal);
+            if (!pass.rec) {  // else launch_scaled_recurrences filled this pass's slot
+                e = cudaFuncSetAttribute(scaled_recurrence_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)sizeof(RecSmem));
+                if (e != cudaSuccess) return e;
+                scaled_recurrence_kernel<<<1, 64, sizeof(RecSmem), stream>>>(
+                    (const double*)grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers, slot,
+                    scaled_slot_bytes(pass.n_loc));
+            }
             const int64_t total = n_chunks * Sh::CH * Sh::G;
             int64_t tb_blocks = (total + 255) / 256;
             if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;

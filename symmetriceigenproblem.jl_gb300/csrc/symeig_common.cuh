@@ -117,7 +117,15 @@ struct ApplyPass {
     int64_t rs = 1;  // stride between the kernel's rows (1: rmul!, lda: lmul! on the transpose)
     int32_t form = 0;  // 0 canonical rotations, 1 the scaled form (FP64 only; see apply.cu)
     int32_t stall = 0; // test hook: > 0 stops the table copies from that chunk on (see wave_tile)
+    int32_t rec = 0;   // form 1: 1 if launch_scaled_recurrences already filled scratch slot `slot`
+    int32_t slot = 0;  // form 1: the pass's scratch slot (its index within the flush)
 };
+
+// The scaled form's column-scale recurrences of all passes of [L0, L0 + layers) in one launch
+// (one CTA per pass of 64 layers), into the scratch slots after the table.
+cudaError_t launch_scaled_recurrences(const double* grid, int64_t grid_rows, const int32_t* place,
+                                      int64_t c0, int64_t n_loc, int64_t L0, int64_t layers,
+                                      void* table, cudaStream_t stream);
 
 // Layers one pass of the wave-window kernel handles for element type T.
 template <typename T> int64_t apply_layers_per_pass();
