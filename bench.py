@@ -451,6 +451,22 @@ def side_measurements(pkg, lib, h, dev, stream, args):
     out["solve_n2000"] = {"seconds": round(dt, 3), "converged": conv, "iter": it,
                           "chase_ms": round(st["chase_ms"], 1), "apply_ms": round(st["apply_ms"], 1),
                           "rotations": st["rotations"], "resid_rel": resid, "orth": orth}
+    # the same solve with the multishift chase (chase mode 3: the reference's error bounds,
+    # another sweep sequence)
+    H = pkg.SymTridiagonal(d.copy(), e.copy())
+    Qh = np.asfortranarray(np.eye(nn))
+    h.set_stream(None)
+    t0 = time.perf_counter()
+    _, conv, it = pkg.qr_algorithm_(H, Qh, handle=h, chase_mode=3)
+    dt = time.perf_counter() - t0
+    st = h.stats()
+    h.set_stream(stream.cuda_stream)
+    resid = float(np.linalg.norm(T @ Qh - Qh * H.dv) / np.linalg.norm(T))
+    orth = float(np.linalg.norm(Qh.T @ Qh - np.eye(nn)))
+    out["solve_n2000_multishift"] = {"seconds": round(dt, 3), "converged": conv, "iter": it,
+                                     "chase_ms": round(st["chase_ms"], 1), "apply_ms": round(st["apply_ms"], 1),
+                                     "rotations": st["rotations"], "bulge_batches": st["bulge_batches"],
+                                     "resid_rel": resid, "orth": orth, "bound_10n_eps": 10 * nn * 2.220446049250313e-16}
     return out
 
 
@@ -795,7 +811,8 @@ def run_dense(args):
         V = pkg.orgtr(tA, tau, handle=h)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
-        _, conv, it = pkg.qr_algorithm_(pkg.SymTridiagonal(d, e), V, handle=h)
+        _, conv, it = pkg.qr_algorithm_(pkg.SymTridiagonal(d, e), V, handle=h, chase_mode=args.chase_mode,
+                                        apply_form=1 if args.form == "scaled" else 0)
         torch.cuda.synchronize()
         t3 = time.perf_counter()
     lam = d
@@ -812,7 +829,8 @@ def run_dense(args):
         "metric": f"dense symmetric eigensolve seconds, n={n}",
         "value": round(t3 - t0, 3), "unit": "s", "higher_is_better": False, "n_gpus": 1, "dtype": "f64",
         "data": "synthetic (seed 5: symmetric, N(0,1) entries)",
-        "config": {"workload": "syev: sytrd -> orgtr -> qr_algorithm!", "n": n},
+        "config": {"workload": "syev: sytrd -> orgtr -> qr_algorithm!", "n": n, "chase_mode": args.chase_mode,
+                   "form": args.form},
         "sytrd_s": round(t1 - t0, 3), "orgtr_s": round(t2 - t1, 3), "qr_s": round(t3 - t2, 3),
         "sytrd_gflops": round(flops / (t1 - t0) / 1e9, 1), "orgtr_gflops": round(flops / (t2 - t1) / 1e9, 1),
         "dmma_peak_tflops": round(pkg._lib.measure_dmma_peak(0), 3),
@@ -831,6 +849,13 @@ def run_dense(args):
                                "kind": "LAPACK (scipy dsytrd + dorgtr)", "sytrd_s": round(t1 - t0, 3),
                                "orgtr_s": round(t2 - t1, 3),
                                "sample": f"the same n={n} matrix, scipy's LAPACK on all host cores"}
+        # the whole dense eigensolve on the host: LAPACK dsyevd (eigenvalues and vectors)
+        from scipy.linalg import eigh
+        t0 = time.perf_counter()
+        eigh(A, driver="evd", check_finite=False)
+        out["cpu_eigh"] = {"value": round(time.perf_counter() - t0, 3), "unit": "s", "cores": os.cpu_count(),
+                           "kind": "LAPACK dsyevd (scipy.linalg.eigh, driver evd)",
+                           "sample": f"the same n={n} matrix, all host cores"}
     print(json.dumps(out), flush=True)
     h.close()
 
