@@ -279,6 +279,8 @@ __device__ void sweep_nr_2w(double* __restrict__ dv, double* __restrict__ ev, in
     }
 }
 
+constexpr int kScanUnroll = 8;  // chunks of 32 entries per round of the deflation scan
+
 __device__ __forceinline__ int32_t warp_max(int32_t v)
 {
 #pragma unroll
@@ -649,13 +651,27 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
             } else if (to <= start) {
                 d.action = 0;
             } else {
-                // from = largest j+1 with is_small(j), j in [start, to-1]; start if none
+                // from = largest j+1 with is_small(j), j in [start, to-1]; start if none.
+                // kScanUnroll chunks of 32 per round: their loads are issued together, so a
+                // long block costs one memory latency per 32 * kScanUnroll entries.
                 int64_t from = start;
-                for (int64_t base = to - 1; base >= start; base -= 32) {
-                    const int64_t j = base - lane;
-                    const bool sm = (j >= start) && is_small(dv, ev, j, tol);
-                    const unsigned mask = __ballot_sync(0xffffffffu, sm);
-                    if (mask) { from = base - (__ffs(mask) - 1) + 1; break; }
+                for (int64_t base = to - 1; base >= start; base -= 32 * kScanUnroll) {
+                    bool sm[kScanUnroll];
+#pragma unroll
+                    for (int u = 0; u < kScanUnroll; ++u) {
+                        const int64_t j = base - 32 * u - lane;
+                        sm[u] = (j >= start) && is_small(dv, ev, j, tol);
+                    }
+                    bool found = false;
+#pragma unroll
+                    for (int u = 0; u < kScanUnroll; ++u) {
+                        const unsigned mask = __ballot_sync(0xffffffffu, sm[u]);
+                        if (!found && mask) {
+                            from = base - 32 * u - (__ffs(mask) - 1) + 1;
+                            found = true;
+                        }
+                    }
+                    if (found) break;
                 }
                 if (from == to) {
                     if (lane == 0) ev[from - 2] = 0.0;
@@ -663,6 +679,7 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
                     to -= 1;
                 } else {
                     int32_t mx = 0;
+#pragma unroll 8
                     for (int64_t q = from - 1 + lane; q <= to - 1; q += 32) mx = max(mx, thick[q]);
                     mx = warp_max(mx);
                     if (mx == max_layers) {
@@ -672,6 +689,7 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
                         bool go = true;
                         if (exact) {
                             int32_t L = 0;
+#pragma unroll 8
                             for (int64_t q = from - 1 + lane; q <= to - 2; q += 32) L = max(L, place[q]);
                             L = warp_max(L);
                             if (to <= n - 1) L = max(L, place[to - 1]);
