@@ -56,6 +56,11 @@ struct symeig_context {
     cudaEvent_t ev_chased[2] = {nullptr, nullptr};
     cudaEvent_t ev_consumed[2] = {nullptr, nullptr};
     cudaEvent_t ev_main = nullptr;
+    // the pipelined host-pointer apply: one stream and completion event per row block, and the
+    // event after the table (created on first use)
+    cudaStream_t pipe[kPipeBlocks] = {};
+    cudaEvent_t pipe_done[kPipeBlocks] = {};
+    cudaEvent_t ev_table = nullptr;
     DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs, bak, rot, dense, dense_io, bulge;
     int* derr = nullptr;   // device error word of the wave kernels (bounded waits)
     int32_t exact_order = 1;  // rotation placement of the qr driver
@@ -396,6 +401,67 @@ int apply_dev(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T*
     return apply_grid<T, T>(h, A, lda, m, cs, n - 1, nullptr, 0, n, k, h->stream);
 }
 
+// One pass (k <= 64 layers) with host Q, pipelined over kPipeBlocks row blocks: column
+// rotations act on every row alike, so rows [r0, r1) of Q are an independent problem.  Each
+// block has its own stream: its host-to-device copy starts at once, its wave kernel waits for
+// the one table (built on the main stream from the (c,s) grid), and its device-to-host copy
+// follows its kernel.  Copies in both directions then overlap the kernels of other blocks, so
+// the call costs about one kernel plus one block's copies instead of both copies plus the
+// kernel.  A single block already fills the FP64 units (2048 rows of 16384 are 128 CTAs of
+// 4 warps: 3.4 warps per SM).
+template <typename T>
+int apply_host_pipelined(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T* cs, int64_t k)
+{
+    cudaStream_t s = h->stream;
+    begin_call(h);
+    for (int b = 0; b < kPipeBlocks; ++b) {
+        if (!h->pipe[b]) CK(cudaStreamCreateWithFlags(&h->pipe[b], cudaStreamNonBlocking));
+        if (!h->pipe_done[b]) CK(cudaEventCreateWithFlags(&h->pipe_done[b], cudaEventDisableTiming));
+    }
+    if (!h->ev_table) CK(cudaEventCreateWithFlags(&h->ev_table, cudaEventDisableTiming));
+    T* q = (T*)h->q.ptr;
+    // the blocks start after whatever the caller queued on the main stream before this call
+    CK(cudaEventRecord(h->ev_main, s));
+    const size_t cs_bytes = (size_t)(n - 1) * k * 2 * sizeof(T);
+    CK(cudaMemcpyAsync(h->cs.ptr, cs, cs_bytes, cudaMemcpyHostToDevice, s));
+    CK(h->table.ensure(apply_table_bytes<T>(n, k)));
+    ApplyPass pass{0, n, 0, k, 1};
+    pass.form = sizeof(T) == 8 ? h->apply_form : 0;
+    pass.stall = h->test_stall;
+    CK((apply_pass<T, T>(q, m, m, (const T*)h->cs.ptr, n - 1, nullptr, pass, h->table.ptr, h->derr, s,
+                         nullptr, nullptr, kPassTable)));
+    CK(cudaEventRecord(h->ev_table, s));
+    // copies in and kernels of every block first, then the copies out: a copy to pageable host
+    // memory blocks the calling thread, and must not hold back the next block's copy in
+    const int64_t rows = ((m + kPipeBlocks - 1) / kPipeBlocks + 63) / 64 * 64;
+    int used = 0;
+    for (int b = 0; b < kPipeBlocks; ++b) {
+        const int64_t r0 = (int64_t)b * rows;
+        if (r0 >= m) break;
+        const int64_t mb = std::min(rows, m - r0);
+        cudaStream_t sb = h->pipe[b];
+        CK(cudaStreamWaitEvent(sb, h->ev_main, 0));
+        CK(cudaMemcpy2DAsync(q + r0, m * sizeof(T), A + r0, lda * sizeof(T), mb * sizeof(T), n,
+                             cudaMemcpyHostToDevice, sb));
+        CK(cudaStreamWaitEvent(sb, h->ev_table, 0));
+        CK((apply_pass<T, T>(q + r0, m, mb, (const T*)h->cs.ptr, n - 1, nullptr, pass, h->table.ptr, h->derr,
+                             sb, nullptr, nullptr, kPassWave)));
+        ++used;
+    }
+    for (int b = 0; b < used; ++b) {
+        const int64_t r0 = (int64_t)b * rows;
+        const int64_t mb = std::min(rows, m - r0);
+        cudaStream_t sb = h->pipe[b];
+        CK(cudaMemcpy2DAsync(A + r0, lda * sizeof(T), q + r0, m * sizeof(T), mb * sizeof(T), n,
+                             cudaMemcpyDeviceToHost, sb));
+        CK(cudaEventRecord(h->pipe_done[b], sb));
+    }
+    for (int b = 0; b < used; ++b) CK(cudaStreamWaitEvent(s, h->pipe_done[b], 0));
+    h->stats.wave_launches += used;
+    h->stats.applied_rotation_rows += (n - 1) * k * m;
+    return SYMEIG_OK;
+}
+
 template <typename T>
 int apply_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T* cs, int64_t k)
 {
@@ -406,11 +472,26 @@ int apply_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T
     if (rc) return rc;
     if (n >= 2 && k > 0 && !cs) return SYMEIG_ERR_NULL;
     if (m == 0 || n < 2 || k == 0) return SYMEIG_OK;
+    if (mul_overflows(n, k * 2)) return SYMEIG_ERR_SIZE;
     auto t0 = std::chrono::steady_clock::now();
     cudaStream_t s = h->stream;
     CK(h->q.ensure((size_t)m * n * sizeof(T)));
     const size_t cs_bytes = (size_t)(n - 1) * k * 2 * sizeof(T);
     CK(h->cs.ensure(cs_bytes));
+    if (k <= apply_layers_per_pass<T>() && m >= (int64_t)kPipeBlocks * 256 && !h->kernel_timing) {
+        rc = apply_host_pipelined<T>(h, A, lda, m, n, cs, k);
+        if (rc) {
+            // nothing queued may still read or write the caller's buffer after the return
+            for (int b = 0; b < kPipeBlocks; ++b)
+                if (h->pipe[b]) cudaStreamSynchronize(h->pipe[b]);
+            cudaStreamSynchronize(s);
+            return rc;
+        }
+        CK(cudaStreamSynchronize(s));
+        h->stats.total_ms =
+            std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        return check_device_error(h);
+    }
     CK(cudaMemcpyAsync(h->cs.ptr, cs, cs_bytes, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpy2DAsync(h->q.ptr, m * sizeof(T), A, lda * sizeof(T), m * sizeof(T), n,
                          cudaMemcpyHostToDevice, s));
@@ -580,8 +661,16 @@ int symeig_destroy(symeig_handle h)
     }
     h->table.release(); h->state.release(); h->d.release(); h->e.release();
     h->q.release(); h->cs.release(); h->bak.release(); h->rot.release();
-    h->dense.release(); h->dense_io.release();
+    h->dense.release(); h->dense_io.release(); h->bulge.release();
     if (h->ev_main) cudaEventDestroy(h->ev_main);
+    for (int b = 0; b < kPipeBlocks; ++b) {
+        if (h->pipe[b]) {
+            cudaStreamSynchronize(h->pipe[b]);
+            cudaStreamDestroy(h->pipe[b]);
+        }
+        if (h->pipe_done[b]) cudaEventDestroy(h->pipe_done[b]);
+    }
+    if (h->ev_table) cudaEventDestroy(h->ev_table);
     for (cudaEvent_t ev : h->timing) cudaEventDestroy(ev);
     for (cudaEvent_t ev : h->kpool) cudaEventDestroy(ev);
     if (h->h_state) cudaFreeHost(h->h_state);

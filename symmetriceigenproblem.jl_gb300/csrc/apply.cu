@@ -350,10 +350,12 @@ template size_t apply_canonical_table_bytes<float>(int64_t);
 template <typename Tsrc, typename T, int S>
 cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t grid_rows,
                              const int32_t* place, const ApplyPass& pass, void* table, int* err,
-                             cudaStream_t stream, cudaEvent_t ev_begin, cudaEvent_t ev_end)
+                             cudaStream_t stream, cudaEvent_t ev_begin, cudaEvent_t ev_end, int what)
 {
     using Sh = typename Cfg<T, S>::Sh;
-    if (m <= 0 || pass.n_loc < 2 || pass.layers <= 0) return cudaSuccess;
+    if (pass.n_loc < 2 || pass.layers <= 0) return cudaSuccess;
+    if (m <= 0 && what != kPassTable) return cudaSuccess;
+    const bool prep = (what & kPassTable) != 0, run = (what & kPassWave) != 0;
     const int64_t n_chunks = Sh::chunks(pass.n_loc);
     const int64_t blocks = (m + Sh::ROWS - 1) / Sh::ROWS;
     cudaError_t e;
@@ -365,22 +367,25 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
             unsigned char* form = slot + scaled_pre_bytes(pass.n_loc);
             double* dfinal = (double*)(form + scaled_form_bytes(pass.n_loc));
             static_assert(sizeof(Tsrc) == 8, "the scaled form reads an FP64 grid");
-            if (!pass.rec) {  // else launch_scaled_recurrences filled this pass's slot
-                e = cudaFuncSetAttribute(scaled_recurrence_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)sizeof(RecSmem));
+            if (prep) {
+                if (!pass.rec) {  // else launch_scaled_recurrences filled this pass's slot
+                    e = cudaFuncSetAttribute(scaled_recurrence_kernel,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RecSmem));
+                    if (e != cudaSuccess) return e;
+                    scaled_recurrence_kernel<<<1, 64, sizeof(RecSmem), stream>>>(
+                        (const double*)grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers, slot,
+                        scaled_slot_bytes(pass.n_loc));
+                }
+                const int64_t total = n_chunks * Sh::CH * Sh::G;
+                int64_t tb_blocks = (total + 255) / 256;
+                if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;
+                scaled_table_kernel<Tsrc, S><<<(unsigned)tb_blocks, 256, 0, stream>>>(
+                    tb, n_chunks, grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers,
+                    pre, form, dfinal);
+                e = cudaGetLastError();
                 if (e != cudaSuccess) return e;
-                scaled_recurrence_kernel<<<1, 64, sizeof(RecSmem), stream>>>(
-                    (const double*)grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers, slot,
-                    scaled_slot_bytes(pass.n_loc));
             }
-            const int64_t total = n_chunks * Sh::CH * Sh::G;
-            int64_t tb_blocks = (total + 255) / 256;
-            if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;
-            scaled_table_kernel<Tsrc, S><<<(unsigned)tb_blocks, 256, 0, stream>>>(
-                tb, n_chunks, grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers,
-                pre, form, dfinal);
-            e = cudaGetLastError();
-            if (e != cudaSuccess) return e;
+            if (!run) return cudaSuccess;
             if (ev_begin) cudaEventRecord(ev_begin, stream);
             wave_apply_kernel<T, S, true><<<(unsigned)blocks, kThreads, 0, stream>>>(
                 Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
@@ -390,14 +395,17 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
             return e;
         }
     }
-    const int64_t total = n_chunks * Sh::CH * Sh::G * Sh::KB;
-    int64_t tb_blocks = (total + 255) / 256;
-    if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;
-    build_table_kernel<Tsrc, T, S><<<(unsigned)tb_blocks, 256, 0, stream>>>(
-        (unsigned char*)table, n_chunks, grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0,
-        pass.layers);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
+    if (prep) {
+        const int64_t total = n_chunks * Sh::CH * Sh::G * Sh::KB;
+        int64_t tb_blocks = (total + 255) / 256;
+        if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;
+        build_table_kernel<Tsrc, T, S><<<(unsigned)tb_blocks, 256, 0, stream>>>(
+            (unsigned char*)table, n_chunks, grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0,
+            pass.layers);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (!run) return cudaSuccess;
     if (ev_begin) cudaEventRecord(ev_begin, stream);
     wave_apply_kernel<T, S><<<(unsigned)blocks, kThreads, 0, stream>>>(
         Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
@@ -410,22 +418,22 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
 template <typename Tsrc, typename T>
 cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t grid_rows,
                        const int32_t* place, const ApplyPass& pass, void* table, int* err,
-                       cudaStream_t stream, cudaEvent_t ev_begin, cudaEvent_t ev_end)
+                       cudaStream_t stream, cudaEvent_t ev_begin, cudaEvent_t ev_end, int what)
 {
     const int s = shape_index<T>();
     if constexpr (sizeof(T) == 4) {
         if (s == 2)
             return apply_pass_shape<Tsrc, T, 2>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
-                                                stream, ev_begin, ev_end);
+                                                stream, ev_begin, ev_end, what);
         if (s == 3)
             return apply_pass_shape<Tsrc, T, 3>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
-                                                stream, ev_begin, ev_end);
+                                                stream, ev_begin, ev_end, what);
     }
     if (s == 0)
         return apply_pass_shape<Tsrc, T, 0>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
-                                            stream, ev_begin, ev_end);
+                                            stream, ev_begin, ev_end, what);
     return apply_pass_shape<Tsrc, T, 1>(Q, ldq, m, grid, grid_rows, place, pass, table, err, stream,
-                                        ev_begin, ev_end);
+                                        ev_begin, ev_end, what);
 }
 
 int apply_num_shapes(int fp64) { return kShapes[fp64 ? 0 : 1]; }
@@ -436,10 +444,10 @@ void apply_set_shape(int fp64, int shape)
 int apply_get_shape(int fp64) { return g_shape[fp64 ? 0 : 1]; }
 
 template cudaError_t apply_pass<double, double>(double*, int64_t, int64_t, const double*, int64_t,
-    const int32_t*, const ApplyPass&, void*, int*, cudaStream_t, cudaEvent_t, cudaEvent_t);
+    const int32_t*, const ApplyPass&, void*, int*, cudaStream_t, cudaEvent_t, cudaEvent_t, int);
 template cudaError_t apply_pass<float, float>(float*, int64_t, int64_t, const float*, int64_t,
-    const int32_t*, const ApplyPass&, void*, int*, cudaStream_t, cudaEvent_t, cudaEvent_t);
+    const int32_t*, const ApplyPass&, void*, int*, cudaStream_t, cudaEvent_t, cudaEvent_t, int);
 template cudaError_t apply_pass<double, float>(float*, int64_t, int64_t, const double*, int64_t,
-    const int32_t*, const ApplyPass&, void*, int*, cudaStream_t, cudaEvent_t, cudaEvent_t);
+    const int32_t*, const ApplyPass&, void*, int*, cudaStream_t, cudaEvent_t, cudaEvent_t, int);
 
 }  // namespace symeig

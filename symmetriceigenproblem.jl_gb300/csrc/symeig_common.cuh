@@ -112,6 +112,14 @@ struct ChaseState {
 // ---- launch helpers (defined in the .cu files) ------------------------------------------
 // Apply geometry of one pass of the wave-window kernel: columns [c0, c0 + n_loc) of Q and
 // layers [L0, L0 + layers) of the (n-1) x * rotation grid.
+// Parts of a pass that apply_pass launches: the table (with the scaled form's recurrence), the
+// wave kernel over the m rows given, or both.  A table built once serves launches over
+// disjoint row ranges of Q on several streams.
+enum : int { kPassTable = 1, kPassWave = 2, kPassAll = 3 };
+
+// Row blocks (and streams) of the pipelined host-pointer apply.
+constexpr int kPipeBlocks = 8;
+
 struct ApplyPass {
     int64_t c0, n_loc, L0, layers;
     int64_t rs = 1;  // stride between the kernel's rows (1: rmul!, lda: lmul! on the transpose)
@@ -147,7 +155,7 @@ template <typename Tsrc, typename T>
 cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t grid_rows,
                        const int32_t* thick, const ApplyPass& pass, void* table, int* err,
                        cudaStream_t stream, cudaEvent_t ev_begin = nullptr,
-                       cudaEvent_t ev_end = nullptr);
+                       cudaEvent_t ev_end = nullptr, int what = kPassAll);
 
 // Tile shape of the single-matrix wave kernel per precision (see apply.cu).
 void apply_set_shape(int fp64, int shape);

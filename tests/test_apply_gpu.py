@@ -47,6 +47,36 @@ def test_apply_host_buffers_with_leading_dimension(cuda, pkg, oracle, dtype):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("m,n,k,ld", [(2100, 300, 64, 2100), (4099, 129, 40, 4111), (2048, 70, 1, 2048),
+                                      (2600, 200, 65, 2600)])
+def test_apply_host_pipelined_row_blocks(cuda, pkg, oracle, m, n, k, ld, dtype):
+    """Host Q with k <= 64 and m >= 2048 runs as 8 row blocks on 8 streams (copy in, kernel,
+    copy out each), all sharing one table; the result is the oracle's bits, the rows beyond m
+    of a leading dimension are untouched.  k = 65 takes the unpipelined path."""
+    rng = np.random.default_rng(m + n + k)
+    big = np.asfortranarray((rng.random((ld, n)) * 2 - 1).astype(dtype))
+    A = big[:m, :]
+    g = rotation_grid(pkg, rng, n, k, dtype)
+    ref = np.asfortranarray(A.copy())
+    oracle.apply_seq(ref, g)
+    untouched = big[m:, :].copy()
+    pkg.bulk_wave_order_2x2_rmul_(A, g)
+    assert np.array_equal(A, ref)
+    assert np.array_equal(big[m:, :], untouched)
+
+
+def test_apply_host_pipelined_scaled_form(cuda, pkg, oracle):
+    rng = np.random.default_rng(77)
+    m, n, k = 2304, 257, 64
+    A = np.asfortranarray(rng.random((m, n)) * 2 - 1)
+    g = rotation_grid(pkg, rng, n, k, np.float64)
+    ref = A.copy(order="F")
+    oracle.apply_scaled(ref, g)
+    pkg.bulk_wave_order_2x2_rmul_(A, g, form=1)
+    assert np.array_equal(A, ref)
+
+
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("m,n,k", [(2, 1, 1), (9, 5, 3), (65, 40, 64), (130, 33, 70)])
 def test_left_apply_matches_oracle(cuda, pkg, oracle, m, n, k, dtype):
     """Bulk lmul! (row rotations) == the oracle's column rotations of the transpose."""
