@@ -195,8 +195,9 @@ int symeig_qr_batched_f64_dev(symeig_handle h, int64_t count, const int64_t* n, 
 int symeig_batched_autotune(symeig_handle h, double* ms);
 /* Read (set = 0) or write (set != 0) the tile shape of the single-matrix wave kernel for FP64
  * (fp64 != 0) or FP32: 0 = 8 lane groups of 8 layers (4 rows per warp), 1 = 4 groups of 16
- * layers (8 rows per warp); FP32 only: 2 = shape 1 and 3 = shape 0 with two rows per thread.
- * Defaults: FP64 0, FP32 2.  Returns SYMEIG_ERR_SIZE for a shape the precision lacks.
+ * layers (8 rows per warp); FP32 only: 2 = shape 1 and 3 = shape 0 with two rows per thread;
+ * FP64 only: 2 = shape 0 in CTAs of 27 warps (108 rows, one CTA per SM at m = 16384); FP64
+ * shape 0 itself runs as 2 when m >= 15000.  Defaults: FP64 0, FP32 2.  Returns SYMEIG_ERR_SIZE for a shape the precision lacks.
  * Process-wide.  No reference counterpart. */
 int symeig_apply_tuning(int32_t fp64, int32_t* shape, int32_t set);
 /* Read (set = 0) or write (set != 0) the batched tuning: class split and shape per class. */

@@ -32,17 +32,24 @@ using wave::kThreads;
 //             rotation-row, and each thread has two independent rotation chains.  Shape 2
 //             is the FP32 choice (1.5-3 % ahead of shape 1, measured).
 template <typename T, int S> struct Cfg;
-template <> struct Cfg<double, 0> { using Sh = Shape<double, 8, 8>; static constexpr int MINB = 7; };
-template <> struct Cfg<double, 1> { using Sh = Shape<double, 16, 4>; static constexpr int MINB = 4; };
-template <> struct Cfg<float, 0> { using Sh = Shape<float, 8, 8>; static constexpr int MINB = 7; };
-template <> struct Cfg<float, 1> { using Sh = Shape<float, 16, 4>; static constexpr int MINB = 5; };
-template <> struct Cfg<float, 2> { using Sh = Shape<float, 16, 4, 2>; static constexpr int MINB = 3; };
-template <> struct Cfg<float, 3> { using Sh = Shape<float, 8, 8, 2>; static constexpr int MINB = 4; };
+template <> struct Cfg<double, 0> { using Sh = Shape<double, 8, 8>; static constexpr int MINB = 7; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<double, 1> { using Sh = Shape<double, 16, 4>; static constexpr int MINB = 4; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<float, 0> { using Sh = Shape<float, 8, 8>; static constexpr int MINB = 7; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<float, 1> { using Sh = Shape<float, 16, 4>; static constexpr int MINB = 5; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<float, 2> { using Sh = Shape<float, 16, 4, 2>; static constexpr int MINB = 3; static constexpr int THREADS = Sh::THREADS; };
+// FP64 shape 2 = shape 0 in one CTA of 27 warps (108 rows): at m = 16384 that is 152 CTAs, one
+// per SM, every SM with the same rows, where 1024 CTAs of 16 rows leave 112 SMs with 7 CTAs and
+// 40 with 6 (the kernel's time is the busiest SM's).  27 warps x 72 registers fit one SM.
+template <> struct Cfg<double, 2> { using Sh = Shape<double, 8, 8, 1, 27>; static constexpr int MINB = 1; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<float, 3> { using Sh = Shape<float, 8, 8, 2>; static constexpr int MINB = 4; static constexpr int THREADS = Sh::THREADS; };
 // the table depends on (KB, G) only, so shapes 2 and 3 share the tables of 1 and 0
 static_assert(Cfg<float, 2>::Sh::CHUNK == Cfg<float, 1>::Sh::CHUNK, "table layout");
 static_assert(Cfg<float, 3>::Sh::CHUNK == Cfg<float, 0>::Sh::CHUNK, "table layout");
+static_assert(Cfg<double, 2>::Sh::CHUNK == Cfg<double, 0>::Sh::CHUNK, "table layout");
 
-constexpr int kShapes[2] = {2, 4};  // shapes available to [0] FP64, [1] FP32
+constexpr int kShapes[2] = {3, 4};  // shapes available to [0] FP64, [1] FP32
+// FP64 shape 0 runs as shape 2 from this many rows on (about 152 SMs x 108 rows x 0.92)
+constexpr int64_t kWideRows = 15000;
 int g_shape[2] = {0, 2};            // [0] FP64, [1] FP32
 template <typename T> int shape_index() { return g_shape[sizeof(T) == 8 ? 0 : 1]; }
 
@@ -285,7 +292,7 @@ scaled_table_kernel(unsigned char* __restrict__ table, int64_t n_chunks, const T
 }
 
 template <typename T, int S, bool SCALED = false>
-__global__ void __launch_bounds__(kThreads, Cfg<T, S>::MINB)
+__global__ void __launch_bounds__(Cfg<T, S>::THREADS, Cfg<T, S>::MINB)
 wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
                   const unsigned char* __restrict__ table, int32_t n_chunks, int* __restrict__ err,
                   const T nz, int64_t rs, int32_t stall)
@@ -387,7 +394,7 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
             }
             if (!run) return cudaSuccess;
             if (ev_begin) cudaEventRecord(ev_begin, stream);
-            wave_apply_kernel<T, S, true><<<(unsigned)blocks, kThreads, 0, stream>>>(
+            wave_apply_kernel<T, S, true><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
                 Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
                 (int32_t)n_chunks, err, (T)-0.0, pass.rs, pass.stall > 0 ? pass.stall : 0x7fffffff);
             e = cudaGetLastError();
@@ -407,7 +414,7 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
     }
     if (!run) return cudaSuccess;
     if (ev_begin) cudaEventRecord(ev_begin, stream);
-    wave_apply_kernel<T, S><<<(unsigned)blocks, kThreads, 0, stream>>>(
+    wave_apply_kernel<T, S><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
         Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
         (int32_t)n_chunks, err, (T)-0.0, pass.rs, pass.stall > 0 ? pass.stall : 0x7fffffff);
     e = cudaGetLastError();
@@ -421,6 +428,12 @@ cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t g
                        cudaStream_t stream, cudaEvent_t ev_begin, cudaEvent_t ev_end, int what)
 {
     const int s = shape_index<T>();
+    if constexpr (sizeof(T) == 8) {
+        // shape 0 takes the 27-warp CTAs of shape 2 once m fills every SM with them
+        if (s == 2 || (s == 0 && m >= kWideRows))
+            return apply_pass_shape<Tsrc, T, 2>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
+                                                stream, ev_begin, ev_end, what);
+    }
     if constexpr (sizeof(T) == 4) {
         if (s == 2)
             return apply_pass_shape<Tsrc, T, 2>(Q, ldq, m, grid, grid_rows, place, pass, table, err,

@@ -1,8 +1,9 @@
 // wave_common.cuh -- the wave-window Givens tile shared by the single-matrix and the batched
 // apply kernels.
 //
-// A tile is the work of one CTA of 4 warps: 4 * R * (32/G) consecutive rows of Q (R rows per
-// thread), all columns of the pass, all G*KB layers of the pass.
+// A tile is the work of one CTA of WARPS warps (4 unless a shape says otherwise): WARPS * R *
+// (32/G) consecutive rows of Q (R rows per thread), all columns of the pass, all G*KB layers
+// of the pass.
 //
 // Order of the rotations.  Rotation (i, L) acts on columns (i, i+1).  The reference's wave
 // order (src/wave.jl:62-162) applies (i, L) after (i-1, L) and after (i+1, L-1); per element
@@ -43,13 +44,14 @@ namespace wave {
 
 constexpr int kThreads = 128;  // 4 warps per CTA
 
-template <typename T, int KB_, int G_, int R_ = 1>
+template <typename T, int KB_, int G_, int R_ = 1, int WARPS_ = kThreads / 32>
 struct Shape {
     using P2 = typename Pair<T>::type;
     static constexpr int KB = KB_, G = G_, W = KB_ + 1;
     static constexpr int R = R_;                                // rows per thread
     static constexpr int RPW = 32 / G;                          // lanes per group
-    static constexpr int ROWS = R * RPW * (kThreads / 32);      // rows per tile
+    static constexpr int THREADS = 32 * WARPS_;                 // threads per CTA
+    static constexpr int ROWS = R * RPW * WARPS_;               // rows per tile
     static constexpr int CH = W;                                // iterations per chunk
     static constexpr int GSTRIDE = KB * (int)sizeof(P2) + 16;   // bytes per group, padded
     static constexpr int ITER = G * GSTRIDE;                    // bytes per iteration

@@ -65,6 +65,21 @@ def test_apply_host_pipelined_row_blocks(cuda, pkg, oracle, m, n, k, ld, dtype):
     assert np.array_equal(big[m:, :], untouched)
 
 
+@pytest.mark.parametrize("m", [15000, 15500, 16417])
+def test_apply_wide_ctas_for_tall_q(cuda, pkg, oracle, m):
+    """From 15000 rows on, FP64 tile shape 0 runs in CTAs of 27 warps (one per SM at 16384
+    rows); the last CTA is partial.  Bits as the oracle's, device path."""
+    rng = np.random.default_rng(m)
+    n, k = 40, 64
+    g = rotation_grid(pkg, rng, n, k, np.float64)
+    A = np.asfortranarray(rng.random((m, n)) * 2 - 1)
+    ref = A.copy(order="F")
+    oracle.apply_seq(ref, g)
+    dA = to_device_colmajor(cuda, A)
+    pkg.bulk_wave_order_2x2_rmul_(dA, cuda.from_numpy(np.ascontiguousarray(g)).cuda())
+    assert np.array_equal(dA.cpu().numpy(), ref)
+
+
 def test_apply_host_pipelined_scaled_form(cuda, pkg, oracle):
     rng = np.random.default_rng(77)
     m, n, k = 2304, 257, 64
@@ -93,11 +108,12 @@ def test_left_apply_matches_oracle(cuda, pkg, oracle, m, n, k, dtype):
     assert np.array_equal(B, refT.T)
 
 
-@pytest.mark.parametrize("dtype,shape", [(np.float64, 0), (np.float64, 1), (np.float32, 0),
+@pytest.mark.parametrize("dtype,shape", [(np.float64, 0), (np.float64, 1), (np.float64, 2), (np.float32, 0),
                                          (np.float32, 1), (np.float32, 2), (np.float32, 3)])
 def test_apply_every_tile_shape(cuda, pkg, oracle, dtype, shape):
     """Every tile shape of the single-matrix wave kernel gives the oracle's bits (FP32 shapes 2
-    and 3 hold two rows per thread; the row counts leave partial tiles and partial warps)."""
+    and 3 hold two rows per thread, FP64 shape 2 is a CTA of 27 warps; the row counts leave
+    partial tiles and partial warps)."""
     import ctypes
     lib = pkg.load_library()
     fp64 = int(dtype == np.float64)
@@ -107,7 +123,7 @@ def test_apply_every_tile_shape(cuda, pkg, oracle, dtype, shape):
     assert lib.symeig_apply_tuning(fp64, ctypes.byref(v), 1) == 0
     try:
         rng = np.random.default_rng(99 + shape)
-        for (m, n, k) in [(33, 70, 64), (100, 129, 130), (7, 20, 5), (77, 40, 64)]:
+        for (m, n, k) in [(33, 70, 64), (100, 129, 130), (7, 20, 5), (77, 40, 64), (333, 90, 64)]:
             g = rotation_grid(pkg, rng, n, k, dtype)
             A = np.asfortranarray((rng.random((m, n)) * 2 - 1).astype(dtype))
             ref = A.copy(order="F")
