@@ -350,6 +350,10 @@ def run_ours(args):
         cpu = {"value": round(gf, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
                "sample": (f"C port of the reference wave kernel, {threads} threads, {shape[0]} of {m} rows "
                           f"x {shape[1]} cols, k={shape[2]}, {dt:.1f} s")}
+        # the same kernel on one thread (a bounded row sample)
+        gf1, _, dt1, shape1 = cpu_wave_gflops(m, n, k, args.dtype, 1, target_s=3.0, max_rows=1024)
+        cpu["one_thread"] = {"value": round(gf1, 3), "unit": "GFLOP/s", "cores": 1,
+                             "sample": f"{shape1[0]} of {m} rows x {shape1[1]} cols, k={shape1[2]}, {dt1:.1f} s"}
 
     if rank == 0:
         line = {
