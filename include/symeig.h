@@ -92,7 +92,7 @@ int symeig_set_chase_mode(symeig_handle h, int32_t mode);
 /* Batch shape of chase mode 3: a batch over a block of len rows runs
  * min(max_bulges, len / rows_per_bulge) bulges (and only when that is at least 2), and each
  * bulge releases its progress to the next every release_every steps.  max_bulges in
- * [2, 64] (default 64), rows_per_bulge >= 4 (default 16), release_every a power of two in
+ * [2, 128] (default 64), rows_per_bulge >= 4 (default 16), release_every a power of two in
  * [1, 64] (default 4).  No reference counterpart. */
 int symeig_set_multishift(symeig_handle h, int32_t max_bulges, int32_t rows_per_bulge,
                           int32_t release_every);

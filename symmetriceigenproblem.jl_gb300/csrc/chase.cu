@@ -290,7 +290,7 @@ __device__ __forceinline__ int32_t warp_max(int32_t v)
 
 // ---- multishift batches (chase_mode 3) -----------------------------------------------------
 //
-// Shifts of a batch of nb <= kMaxBulges = 64 bulges over a block ending at row `to` (1-based):
+// Shifts of a batch of nb <= kMaxBulges bulges over a block ending at row `to` (1-based):
 // the eigenvalues of the block's trailing nb x nb principal submatrix, ascending.  The
 // submatrix is scaled by an exact power of two to max |entry| in [0.5, 1); each eigenvalue
 // is bracketed by bisection on FP32 Sturm counts, then takes up to three FP64 Newton steps on
@@ -298,19 +298,20 @@ __device__ __forceinline__ int32_t warp_max(int32_t v)
 // finite or leaves the FP32 bracket's neighbourhood is refused (clustered roots).  FP32 shifts
 // alone cost about 25 % more sweeps: the bulges' reduction of the trailing couplings is
 // limited by the shifts' distance to the eigenvalues.  All 32 lanes of warp 0 call it; lane l
-// finds eigenvalues l and l + 32; sd, se2, sea (FP32) and dd, ee2 (FP64) are
+// finds eigenvalues l, l + 32, ...; sd, se2, sea (FP32) and dd, ee2 (FP64) are
 // kMaxBulges-entry shared arrays.
 __device__ void batch_shifts(const double* __restrict__ dv, const double* __restrict__ ev,
                              int64_t to, int nb, double* __restrict__ shifts, float* sd, float* se2,
                              float* sea, double* dd, double* ee2)
 {
     const int lane = threadIdx.x & 31;
+    constexpr int H = kMaxBulges / 32;
     const int64_t r0 = to - nb;  // 0-based first row of the submatrix
-    // lane holds entries q = lane and lane + 32 of the submatrix
-    double dq[2], eq[2];
+    // lane holds entries q = lane + 32 h of the submatrix
+    double dq[H], eq[H];
     double mx = 0.0;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < H; ++h) {
         const int q = lane + 32 * h;
         dq[h] = q < nb ? dv[r0 + q] : 0.0;
         eq[h] = q < nb - 1 ? ev[r0 + q] : 0.0;
@@ -321,7 +322,7 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
     if (!(mx > 0.0) || !isfinite(mx)) {
         // a zero block is already diagonal; a non-finite one is left to the sweep
 #pragma unroll
-        for (int h = 0; h < 2; ++h)
+        for (int h = 0; h < H; ++h)
             if (lane + 32 * h < nb) shifts[lane + 32 * h] = dq[h];
         __syncwarp();
         return;
@@ -329,7 +330,7 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
     int ex;
     frexp(mx, &ex);
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < H; ++h) {
         const int q = lane + 32 * h;
         const double dsc = ldexp(dq[h], -ex), esc = ldexp(eq[h], -ex);
         const float ef = (float)esc;
@@ -343,7 +344,7 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
     // Gershgorin interval of the submatrix
     float lo = 3.0f, hi = -3.0f;
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < H; ++h) {
         const int q = lane + 32 * h;
         if (q < nb) {
             const float rad = (q >= 1 ? sea[q - 1] : 0.0f) + (q < nb - 1 ? sea[q] : 0.0f);
@@ -359,7 +360,7 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
     lo -= 1e-6f;
     hi += 1e-6f;
     constexpr float kPiv = 1e-30f;
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < H; ++h) {
         const int k = lane + 32 * h;   // the eigenvalue this lane finds
         if (32 * h >= nb) break;       // uniform
         float a = lo, b = hi;

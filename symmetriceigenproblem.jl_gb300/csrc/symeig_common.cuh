@@ -60,7 +60,7 @@ enum ChaseStatus : int32_t {
 // kDefaultRowsPerBulge, the fastest measured at n = 2000 and 16384), and never more than
 // kMaxBulges.  A bulge releases its progress every kDefaultProgEvery steps; the host queues
 // kBatchesAhead batches per round trip.
-constexpr int kMaxBulges = 64;
+constexpr int kMaxBulges = 128;
 constexpr int kDefaultBulges = 64;
 constexpr int kDefaultRowsPerBulge = 16;
 constexpr int kDefaultProgEvery = 4;

@@ -193,7 +193,7 @@ faster at n = 16384)."""
 set_chase_mode!(mode::Integer) =
     check(:symeig_set_chase_mode, ccall((:symeig_set_chase_mode, libsymeig), Cint, (Ptr{Cvoid}, Int32), handle(), mode))
 
-"""Batch shape of chase mode 3: at most `bulges` (2..64, default 64) bulges per batch, one per
+"""Batch shape of chase mode 3: at most `bulges` (2..128, default 64) bulges per batch, one per
 `rows` (default 16) rows of the block, each releasing its progress every `release` steps
 (a power of two, default 4)."""
 set_multishift!(bulges::Integer = 64, rows::Integer = 16, release::Integer = 4) =

@@ -146,13 +146,13 @@ def test_multishift_fp32_q_and_device_tensors(cuda, pkg):
     assert res <= 10 * n * eps32 and orth <= 10 * n * eps32, (res, orth)
 
 
-@pytest.mark.parametrize("kind,n", [("B", 1500), ("split", 900)])
-def test_multishift_pipelining_is_exact(cuda, pkg, kind, n):
+@pytest.mark.parametrize("kind,n,bulges", [("B", 1500, 64), ("split", 900, 64), ("B", 2500, 128)])
+def test_multishift_pipelining_is_exact(cuda, pkg, kind, n, bulges):
     """For given shifts the pipelined bulges compute what the same sweeps run one after
     another compute: the result does not depend on how far apart the bulges run (a release
     every 1, 8 or 64 steps) -- bit for bit, eigenvalues and Q."""
     d, e = tridiag(kind, n, seed=n + 3)
-    runs = [solve(pkg, d, e, ms=(64, 16, r)) for r in (1, 8, 64)]
+    runs = [solve(pkg, d, e, ms=(bulges, 16, r)) for r in (1, 8, 64)]
     for lam, Q, conv, it, st in runs[1:]:
         assert conv and it == runs[0][3] and st["bulge_batches"] == runs[0][4]["bulge_batches"]
         assert np.array_equal(lam, runs[0][0]) and np.array_equal(Q, runs[0][1])
@@ -162,11 +162,11 @@ def test_multishift_pipelining_is_exact(cuda, pkg, kind, n):
 def test_multishift_settings_are_checked(cuda, pkg):
     h = pkg.Handle(0)
     try:
-        for bad in ((1, 16, 8), (65, 16, 8), (64, 3, 8), (64, 16, 0), (64, 16, 3), (64, 16, 128)):
+        for bad in ((1, 16, 8), (129, 16, 8), (64, 3, 8), (64, 16, 0), (64, 16, 3), (64, 16, 128)):
             with pytest.raises(pkg.SymeigError):
                 h.set_multishift(*bad)
         h.set_multishift(2, 4, 1)
-        h.set_multishift(64, 1 << 20, 64)
+        h.set_multishift(128, 1 << 20, 64)
     finally:
         h.close()
 
