@@ -407,8 +407,8 @@ int apply_dev(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T*
 // the one table (built on the main stream from the (c,s) grid), and its device-to-host copy
 // follows its kernel.  Copies in both directions then overlap the kernels of other blocks, so
 // the call costs about one kernel plus one block's copies instead of both copies plus the
-// kernel.  A single block already fills the FP64 units (2048 rows of 16384 are 128 CTAs of
-// 4 warps: 3.4 warps per SM).
+// kernel.  A single block keeps the FP64 units busy (1024 rows of 16384 are 64 CTAs of 4 warps,
+// and the blocks' kernels overlap one another).
 template <typename T>
 int apply_host_pipelined(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T* cs, int64_t k)
 {

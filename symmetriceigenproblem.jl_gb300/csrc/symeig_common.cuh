@@ -118,7 +118,7 @@ struct ChaseState {
 enum : int { kPassTable = 1, kPassWave = 2, kPassAll = 3 };
 
 // Row blocks (and streams) of the pipelined host-pointer apply.
-constexpr int kPipeBlocks = 8;
+constexpr int kPipeBlocks = 16;
 
 struct ApplyPass {
     int64_t c0, n_loc, L0, layers;

@@ -47,12 +47,12 @@ def test_apply_host_buffers_with_leading_dimension(cuda, pkg, oracle, dtype):
 
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
-@pytest.mark.parametrize("m,n,k,ld", [(2100, 300, 64, 2100), (4099, 129, 40, 4111), (2048, 70, 1, 2048),
-                                      (2600, 200, 65, 2600)])
+@pytest.mark.parametrize("m,n,k,ld", [(4100, 300, 64, 4100), (4099, 129, 40, 4111), (4096, 70, 1, 4096),
+                                      (5000, 200, 65, 5000), (2100, 90, 64, 2100)])
 def test_apply_host_pipelined_row_blocks(cuda, pkg, oracle, m, n, k, ld, dtype):
-    """Host Q with k <= 64 and m >= 2048 runs as 8 row blocks on 8 streams (copy in, kernel,
+    """Host Q with k <= 64 and m >= 4096 runs as 16 row blocks on 16 streams (copy in, kernel,
     copy out each), all sharing one table; the result is the oracle's bits, the rows beyond m
-    of a leading dimension are untouched.  k = 65 takes the unpipelined path."""
+    of a leading dimension are untouched.  k = 65 and m = 2100 take the unpipelined path."""
     rng = np.random.default_rng(m + n + k)
     big = np.asfortranarray((rng.random((ld, n)) * 2 - 1).astype(dtype))
     A = big[:m, :]
@@ -82,7 +82,7 @@ def test_apply_wide_ctas_for_tall_q(cuda, pkg, oracle, m):
 
 def test_apply_host_pipelined_scaled_form(cuda, pkg, oracle):
     rng = np.random.default_rng(77)
-    m, n, k = 2304, 257, 64
+    m, n, k = 4352, 257, 64
     A = np.asfortranarray(rng.random((m, n)) * 2 - 1)
     g = rotation_grid(pkg, rng, n, k, np.float64)
     ref = A.copy(order="F")
