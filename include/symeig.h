@@ -107,8 +107,10 @@ int symeig_set_apply_form(symeig_handle h, int32_t form);
 /* Test hook for the failure path of the bounded device waits: with chunk > 0 the wave
  * kernels stop copying their rotation table from that chunk on, so their waits run out
  * (~2 s of SM clock), the kernels return without touching Q further, and the synchronous
- * entry points return SYMEIG_ERR_TIMEOUT (device_errors = 1 in the statistics).  Q is then
- * unspecified; the handle and the context stay usable.  0 (default) turns it off. */
+ * entry points return SYMEIG_ERR_TIMEOUT (device_errors = 1 in the statistics).  In chase
+ * mode 3 the first bulge of each batch also stops releasing its progress, so the next bulge's
+ * wait runs out the same way.  Q (and, in mode 3, H) is then unspecified; the handle and the
+ * context stay usable.  0 (default) turns it off. */
 int symeig_set_test_stall(symeig_handle h, int32_t chunk);
 /* Record CUDA events around every wave-kernel launch so symeig_get_stats can report their
  * device time (wave_kernel_ms).  Off by default.  symeig_get_stats waits for the last

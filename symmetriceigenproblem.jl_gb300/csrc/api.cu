@@ -240,6 +240,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     init.ms_bulges = h->ms_bulges;
     init.ms_rows = h->ms_rows;
     init.ms_prog_mask = h->ms_prog_every - 1;
+    init.test_stall = h->test_stall;
     ChaseState* dstate = (ChaseState*)h->state.ptr;
 
     cudaStream_t ms = h->stream, cs = h->chase_stream;

@@ -460,7 +460,7 @@ __device__ void sweep_bulge_2w(double* __restrict__ dv, double* __restrict__ ev,
                                int64_t to, double mu, double* __restrict__ grid,
                                const int32_t* __restrict__ thick, int64_t rows, int32_t layer,
                                int32_t jofs, double nz, NrMail* mail, PipeWait pw,
-                               long long* __restrict__ my_prog, int64_t prog_mask)
+                               long long* __restrict__ my_prog, int64_t prog_mask, bool hold)
 {
     const int warp = threadIdx.x >> 5;
     const bool lead = (threadIdx.x & 31) == 0;
@@ -533,7 +533,7 @@ __device__ void sweep_bulge_2w(double* __restrict__ dv, double* __restrict__ ev,
                     dv[i] = B22pp;
                     ev[i - 1] = __fma_rn(B12p, c, -mulz(B11p, s, nz));
                 }
-                if (i == to - 1 || ((i - from) & prog_mask) == prog_mask) st_release_gpu(my_prog, i);
+                if (!hold && (i == to - 1 || ((i - from) & prog_mask) == prog_mask)) st_release_gpu(my_prog, i);
             }
             B11 = B22pp;
             B21 = e_next;
@@ -561,7 +561,8 @@ bulge_batch_kernel(const ChaseState* __restrict__ st, double* __restrict__ dv,
     const int32_t L0 = st->b_layer0;
     PipeWait pw{j > 0 ? &bs->prog[j - 1] : nullptr, err, -1};
     sweep_bulge_2w(dv, ev, from, to, bs->shifts[j], grid, thick, rows, L0 > 0 ? L0 + j : 0, j,
-                   st->neg_zero, mail, pw, &bs->prog[j], (int64_t)st->ms_prog_mask);
+                   st->neg_zero, mail, pw, &bs->prog[j], (int64_t)st->ms_prog_mask,
+                   st->test_stall != 0 && j == 0);
 }
 
 // One flush: the reference's inner loop from `to = last_block_ends_at` until the matrix is

@@ -106,7 +106,8 @@ struct ChaseState {
     int32_t ms_bulges;           // bulge cap of a batch (2 .. kMaxBulges)
     int32_t ms_rows;             // rows of a block per bulge (>= 4)
     int32_t ms_prog_mask;        // a bulge releases its progress every (mask + 1) steps
-    int32_t pad1;
+    int32_t test_stall;          // test hook (symeig_set_test_stall): bulge 0 of a batch never
+                                 // releases its progress, so the next bulge's wait runs out
 };
 
 // ---- launch helpers (defined in the .cu files) ------------------------------------------

@@ -45,3 +45,37 @@ def test_bounded_wait_timeout_is_reported_and_recoverable(cuda, pkg, oracle):
     oracle.apply_seq(ref, cs)
     assert np.array_equal(A, ref)
     assert h.stats()["device_errors"] == 0
+
+
+def test_multishift_bulge_wait_timeout_is_reported_and_recoverable(cuda, pkg):
+    """Chase mode 3: with the stall hook on, bulge 0 of each batch never releases its progress;
+    the next bulge's bounded wait runs out (~2 s), sets the error word, and every later wait
+    gives up at once, so the call ends (here at maxiter = 50) and reports SYMEIG_ERR_TIMEOUT.
+    No GPU fault: every index is independent of the values read.  The same handle then
+    solves correctly."""
+    from scipy.linalg import eigh_tridiagonal
+    lib = pkg.load_library()
+    h = pkg.Handle(0)
+    try:
+        rng = np.random.default_rng(5)
+        n = 600
+        d, e = rng.standard_normal(n), rng.random(n - 1)
+        eps = np.finfo(np.float64).eps
+        conv, it = ctypes.c_int32(), ctypes.c_int64()
+        h.set_chase_mode(3)
+        assert lib.symeig_set_test_stall(h.ptr, 1) == 0
+        dd, ee = d.copy(), e.copy()
+        rc = lib.symeig_qr_f64(h.ptr, dd.ctypes.data, ee.ctypes.data, n, None, 1, 0, 128, eps, 50,
+                               ctypes.byref(conv), ctypes.byref(it))
+        assert rc == SYMEIG_ERR_TIMEOUT
+        assert h.stats()["device_errors"] == 1 and h.stats()["bulge_batches"] > 0
+        assert lib.symeig_set_test_stall(h.ptr, 0) == 0
+        dd, ee = d.copy(), e.copy()
+        rc = lib.symeig_qr_f64(h.ptr, dd.ctypes.data, ee.ctypes.data, n, None, 1, 0, 128, eps, 100 * n,
+                               ctypes.byref(conv), ctypes.byref(it))
+        assert rc == 0 and conv.value == 1 and h.stats()["device_errors"] == 0
+        ref = eigh_tridiagonal(d, e, eigvals_only=True)
+        assert np.max(np.abs(np.sort(dd) - ref)) <= 10 * n * eps * np.max(np.abs(ref))
+    finally:
+        h.set_chase_mode(0)
+        h.close()
