@@ -170,7 +170,8 @@ class Handle:
 
     def set_chase_mode(self, mode):
         """0: Newton-form two-warp chase (default); 1: reference form; 2: Newton form with
-        every sweep redone in the reference form.  All give the same bits."""
+        every sweep redone in the reference form -- these give the reference's bits; 3: the
+        multishift chase (within the reference's error bounds)."""
         check("symeig_set_chase_mode", self._lib.symeig_set_chase_mode(self.ptr, int(mode)))
 
     def set_stream(self, stream_ptr: int | None):

@@ -242,15 +242,17 @@ def qr_algorithm_(H: SymTridiagonal, Q=None, max_layers: int = 128, tol: float |
     return H, bool(conv.value), int(it.value)
 
 
-def eigen_decomp_(H: SymTridiagonal, handle: Handle | None = None):
+def eigen_decomp_(H: SymTridiagonal, handle: Handle | None = None, chase_mode: int = 0,
+                  apply_form: int = 0):
     """eigen_decomp!(H) (src/bulge_chasing.jl:290-299): Q = I, qr_algorithm!, returns
-    (eigenvalues, Q).  The reference returns Diagonal(H.dv); here the 1-D array H.dv."""
+    (eigenvalues, Q).  The reference returns Diagonal(H.dv); here the 1-D array H.dv.
+    chase_mode and apply_form as for qr_algorithm_."""
     n = H.n
     if _is_torch(H.dv):
         Q = torch.eye(n, dtype=torch.float64, device=H.dv.device).T  # column-major view
     else:
         Q = np.asfortranarray(np.eye(n))
-    _, converged, iters = qr_algorithm_(H, Q, handle=handle)
+    _, converged, iters = qr_algorithm_(H, Q, handle=handle, chase_mode=chase_mode, apply_form=apply_form)
     return H.dv, Q
 
 
