@@ -47,7 +47,13 @@
  *   apply (scaled)      The device's optional scaled ("fast Givens") form of the FP64 apply
  *                       (no reference counterpart), restated so that its results can be
  *                       checked bit for bit as well.
+ *   qr multishift       The device's multishift chase (chase mode 3; no reference
+ *                       counterpart): batches of sweeps with the trailing square's
+ *                       eigenvalues as shifts, on the reference's deflation, capacity and
+ *                       placement rules.  Checked by the reference's error bounds, and by the
+ *                       reference's bits where no block takes a batch.
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -496,6 +502,9 @@ typedef struct {
     int64_t early_flushes;      /* flushes ended because a sweep's layer exceeded grid_layers */
     int64_t max_place;          /* thickest grid column of the last flush */
     int64_t min_from, max_to;   /* 1-based column range of the last flush's sweeps */
+    int32_t ms_bulges;          /* multishift batches: bulge cap (0: single shifts only) */
+    int32_t ms_rows;            /* multishift batches: block rows per bulge */
+    int64_t batches;            /* multishift batches run */
 } oracle_qr_state;
 
 void oracle_qr_init(oracle_qr_state* st, int64_t n, int32_t max_layers, double tol, int64_t maxiter,
@@ -506,6 +515,47 @@ void oracle_qr_init(oracle_qr_state* st, int64_t n, int32_t max_layers, double t
     st->start = 1; st->last_block_ends_at = n; st->iter = 0;
     st->exact_order = exact_order;
     st->grid_layers = exact_order ? 2 * max_layers : max_layers;
+}
+
+/* The eigenvalues of the trailing nb x nb principal submatrix of a block ending at row `to`
+ * (1-based), ascending: bisection on Sturm counts (the LDL^T pivots of T - x I, a negative
+ * pivot per eigenvalue below x) down to adjacent doubles.  They are the shifts of a multishift
+ * batch.  The device computes the same eigenvalues to about 1e-16 relative to the block's
+ * norm by FP32 bisection and FP64 Newton steps; shifts only steer convergence, so the two
+ * need not agree in their last bits. */
+static void oracle_trailing_eigenvalues(const double* dv, const double* ev, int64_t to, int nb, double* out)
+{
+    const double* d = dv + (to - nb);
+    const double* e = ev + (to - nb);
+    double lo = INFINITY, hi = -INFINITY, e2max = 0.0;
+    for (int i = 0; i < nb; ++i) {
+        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < nb - 1 ? fabs(e[i]) : 0.0);
+        if (d[i] - r < lo) lo = d[i] - r;
+        if (d[i] + r > hi) hi = d[i] + r;
+        if (i < nb - 1 && e[i] * e[i] > e2max) e2max = e[i] * e[i];
+    }
+    const double pivmin = DBL_MIN * (e2max > 1.0 ? e2max : 1.0);
+    const double w = hi - lo;
+    lo -= 1e-12 * (w > 0.0 ? w : 1.0) + DBL_MIN;
+    hi += 1e-12 * (w > 0.0 ? w : 1.0) + DBL_MIN;
+    for (int k = 0; k < nb; ++k) {
+        double a = lo, b = hi;
+        for (int it = 0; it < 200; ++it) {
+            const double mid = 0.5 * (a + b);
+            if (!(mid > a && mid < b)) break;
+            int cnt = 0;
+            double q = d[0] - mid;
+            if (q < 0.0) ++cnt;
+            for (int i = 1; i < nb; ++i) {
+                if (fabs(q) < pivmin) q = -pivmin;
+                q = (d[i] - mid) - e[i - 1] * e[i - 1] / q;
+                if (q < 0.0) ++cnt;
+            }
+            if (cnt > k) b = mid;
+            else a = mid;
+        }
+        out[k] = 0.5 * (a + b);
+    }
 }
 
 /* One pass of qr_algorithm!'s outer loop up to (not including) the bulk apply
@@ -547,13 +597,36 @@ int oracle_qr_flush(oracle_qr_state* st, double* dv, double* ev, double* givens,
                     layer = sweep_layer(place, n, from, to);
                     if (layer > st->grid_layers) { st->early_flushes += 1; break; }
                 }
-                double mu = oracle_wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
+                /* multishift (the device's chase mode 3): as many sweeps as the block's length,
+                 * its layer room (the capacity rule of that many single sweeps) and maxiter
+                 * allow, with the trailing submatrix's eigenvalues as shifts; the device chases
+                 * them as concurrent bulges, which computes what these sweeps in sequence do */
+                int64_t nbl = 1;
+                if (st->ms_bulges >= 2) {
+                    int64_t cap = (int64_t)st->max_layers - thickness;
+                    if (st->exact_order && (int64_t)st->grid_layers - layer + 1 < cap) cap = st->grid_layers - layer + 1;
+                    nbl = (to - from + 1) / st->ms_rows;
+                    if (nbl > st->ms_bulges) nbl = st->ms_bulges;
+                    if (nbl > cap) nbl = cap;
+                    if (nbl > st->maxiter - st->iter + 1) nbl = st->maxiter - st->iter + 1;
+                }
                 did_a_thing = 1;
-                oracle_single_shift(dv, ev, n, from, to, mu, givens, rows, thick, place, layer);
+                if (nbl >= 2) {
+                    double shifts[128];
+                    oracle_trailing_eigenvalues(dv, ev, to, (int)nbl, shifts);
+                    for (int64_t j = 0; j < nbl; ++j)
+                        oracle_single_shift(dv, ev, n, from, to, shifts[j], givens, rows, thick, place,
+                                            layer > 0 ? layer + j : 0);
+                    st->batches += 1;
+                } else {
+                    double mu = oracle_wilkinson_shift(dv[to - 2], dv[to - 1], ev[to - 2]);
+                    oracle_single_shift(dv, ev, n, from, to, mu, givens, rows, thick, place, layer);
+                    nbl = 1;
+                }
                 if (from < st->min_from) st->min_from = from;
                 if (to > st->max_to) st->max_to = to;
-                st->total_rotations += to - from;
-                st->iter += 1;
+                st->total_rotations += nbl * (to - from);
+                st->iter += nbl;
             }
         }
         if (to <= start) break;
@@ -588,15 +661,47 @@ int oracle_qr(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, 
  * scaled form (apply_form 1, FP64 Q): each flush is applied to the columns its sweeps
  * touched, min_from-1 .. max_to-1, in passes of 64 layers (oracle_apply_scaled_pass_f64),
  * as the device applies it. */
+static int oracle_qr_driver(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
+                            int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
+                            int32_t apply_form, int32_t ms_bulges, int32_t ms_rows, int32_t* converged,
+                            int64_t* iter, int64_t* flushes, int64_t* rotations, int64_t* batches);
+
 int oracle_qr_form(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
                    int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
                    int32_t apply_form, int32_t* converged, int64_t* iter, int64_t* flushes,
                    int64_t* rotations)
 {
+    return oracle_qr_driver(d, e, n, Q, ldq, m, q_is_f32, max_layers, tol, maxiter, exact_order,
+                            apply_form, 0, 16, converged, iter, flushes, rotations, NULL);
+}
+
+/* The device's multishift chase (chase mode 3; not the reference's algorithm, which is
+ * oracle_qr) restated: where a block has room, a batch of up to ms_bulges sweeps
+ * (min(ms_bulges, len / ms_rows), the layer room and maxiter decide) with the eigenvalues of
+ * the block's trailing square as shifts, run as sweeps in sequence with the reference's
+ * rotations; every other decision, the apply and the placement as in oracle_qr.  FP64 Q,
+ * canonical apply.  *batches receives the number of batches. */
+int oracle_qr_multishift(double* d, double* e, int64_t n, double* Q, int64_t ldq, int64_t m,
+                         int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
+                         int32_t ms_bulges, int32_t ms_rows, int32_t* converged, int64_t* iter,
+                         int64_t* flushes, int64_t* rotations, int64_t* batches)
+{
+    if (ms_bulges < 2 || ms_bulges > 128 || ms_rows < 4) return 1;
+    return oracle_qr_driver(d, e, n, Q, ldq, m, 0, max_layers, tol, maxiter, exact_order, 0, ms_bulges,
+                            ms_rows, converged, iter, flushes, rotations, batches);
+}
+
+static int oracle_qr_driver(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
+                            int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
+                            int32_t apply_form, int32_t ms_bulges, int32_t ms_rows, int32_t* converged,
+                            int64_t* iter, int64_t* flushes, int64_t* rotations, int64_t* batches)
+{
     if (apply_form != 0 && q_is_f32) return 1;
     if (n < 1 || max_layers < 1 || (Q && ldq < m)) return 1;
     oracle_qr_state st;
     oracle_qr_init(&st, n, max_layers, tol, maxiter, exact_order);
+    st.ms_bulges = ms_bulges;
+    st.ms_rows = ms_rows;
     int64_t nr = n > 1 ? n - 1 : 1;
     int64_t GL = st.grid_layers;
     double* givens = (double*)malloc(sizeof(double) * 2 * nr * GL);
@@ -631,6 +736,7 @@ int oracle_qr_form(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_
     *iter = st.iter;
     if (flushes) *flushes = st.flush_count;
     if (rotations) *rotations = st.total_rotations;
+    if (batches) *batches = st.batches;
     free(givens); free(g32); free(thick); free(place);
     return 0;
 }
