@@ -401,8 +401,8 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
 }
 
 // The bulges of a batch.  Bulge j (CTA j) runs the two-warp sweep of sweep_nr_2w (same split,
-// mailbox and barriers) with shift shifts[j] over the batch's block, one step behind another
-// bulge's stores: step k of a sweep stores dv[k-1] and ev[k-2] (0-based; its last step also
+// mailbox and barriers) with shift shifts[j] over the batch's block, a few steps behind bulge
+// j-1, reading only what bulge j-1 has stored: step k of a sweep stores dv[k-1] and ev[k-2] (0-based; its last step also
 // dv[k] and ev[k-1]), so before its loads for step i+1 (dv[i+1], ev[i+1]) bulge j needs bulge
 // j-1 through step min(i+3, to-1).  The helper warp's store thread releases the bulge's
 // progress every (prog_mask + 1) steps and at its last step (st.release.gpu); the next bulge's
@@ -414,6 +414,8 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
 // two warps' barrier protocol still completes; the call then reports the error.
 // The rotation is givens_nr_core (reference form out of its range) without the rounding
 // proof: the batch is not the reference's sweep sequence, so there are no bits to match.
+// `hold` (the test hook of symeig_set_test_stall, bulge 0 only) withholds every release, so
+// the next bulge's wait runs out.
 
 __device__ __forceinline__ long long ld_acquire_gpu(const long long* p)
 {
