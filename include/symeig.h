@@ -239,6 +239,20 @@ int symeig_eig_adjoint_f64_dev(symeig_handle h, int64_t count, int64_t n, const 
 #define SYMEIG_NOALLOC_SCRATCH_BYTES (32u << 20)
 int symeig_apply_givens_f64_noalloc(double* A, int64_t lda, int64_t m, int64_t n,
                                     const double* cs, int64_t k, void* stream);
+/* No counterpart in the reference.  The set-up step of symeig_apply_givens_f64_noalloc on
+ * the current device, on its own: under lazy module loading (the CUDA default) the first
+ * use of the entry point's module on a device loads it and claims its device array, which
+ * fails with SYMEIG_ERR_CUDA if another allocator already holds the memory.  Call this once
+ * per device before such an allocator reserves the device and before any stream capture;
+ * it allocates nothing else and is cheap to repeat. */
+int symeig_noalloc_init(void);
+/* No counterpart in the reference.  The allocation-free apply is asynchronous, so its
+ * return value cannot report a bounded wait that gave up inside its kernel (Q is then only
+ * partly rotated).  This waits for `stream` (NULL = legacy default stream, current device),
+ * reads the shared error word of the allocation-free apply on the current device, clears it,
+ * and returns SYMEIG_ERR_TIMEOUT if any call since the last check gave up, else SYMEIG_OK.
+ * It allocates nothing. */
+int symeig_noalloc_status(void* stream);
 
 /* ---- bulk lmul!: row rotations  (src/simple_givens.jl:38-51) --------------------------------- *
  * A (m x n, column-major, lda >= m) <- prod of the (m-1) x k grid of row rotations cs applied

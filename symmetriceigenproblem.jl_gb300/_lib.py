@@ -62,6 +62,8 @@ SIGNATURES = {
     "symeig_apply_givens_left_f64_dev": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
     "symeig_apply_givens_left_f32_dev": (ctypes.c_int, [c_vp, c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]),
     "symeig_apply_givens_f64_noalloc": (ctypes.c_int, [c_vp, c_i64, c_i64, c_i64, c_vp, c_i64, c_vp]),
+    "symeig_noalloc_init": (ctypes.c_int, []),
+    "symeig_noalloc_status": (ctypes.c_int, [c_vp]),
     "symeig_qr_batched_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_dbl, c_i64, c_vp, c_vp]),
     "symeig_qr_batched_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_dbl, c_i64, c_vp, c_vp]),
     "symeig_batched_autotune": (ctypes.c_int, [c_vp, c_vp]),

@@ -246,13 +246,30 @@ def eigen_decomp_(H: SymTridiagonal, handle: Handle | None = None, chase_mode: i
                   apply_form: int = 0):
     """eigen_decomp!(H) (src/bulge_chasing.jl:290-299): Q = I, qr_algorithm!, returns
     (eigenvalues, Q).  The reference returns Diagonal(H.dv); here the 1-D array H.dv.
-    chase_mode and apply_form as for qr_algorithm_."""
+    chase_mode and apply_form as for qr_algorithm_.  Host arrays go through the C entry point
+    symeig_eigen_decomp_f64 (which sets Q = I itself); device tensors through qr_algorithm_."""
     n = H.n
     if _is_torch(H.dv):
         Q = torch.eye(n, dtype=torch.float64, device=H.dv.device).T  # column-major view
-    else:
-        Q = np.asfortranarray(np.eye(n))
-    _, converged, iters = qr_algorithm_(H, Q, handle=handle, chase_mode=chase_mode, apply_form=apply_form)
+        qr_algorithm_(H, Q, handle=handle, chase_mode=chase_mode, apply_form=apply_form)
+        return H.dv, Q
+    for a in (H.dv, H.ev):
+        if not isinstance(a, np.ndarray) or a.dtype != np.float64 or not a.flags.c_contiguous or not a.flags.writeable:
+            raise TypeError("H.dv / H.ev must be writeable contiguous float64 numpy arrays")
+    if H.ev.shape[0] != max(n - 1, 0):
+        raise ValueError("ev must have n-1 entries")
+    Q = np.empty((n, n), dtype=np.float64, order="F")
+    h = handle or default_handle(0)
+    conv, it = c_i32(), c_i64()
+    h.set_chase_mode(chase_mode)
+    h.set_apply_form(apply_form)
+    try:
+        h.call("symeig_eigen_decomp_f64", ctypes.c_void_p(H.dv.ctypes.data),
+               ctypes.c_void_p(H.ev.ctypes.data if H.ev.size else None), n, ctypes.c_void_p(Q.ctypes.data), n,
+               ctypes.byref(conv), ctypes.byref(it))
+    finally:
+        h.set_chase_mode(0)
+        h.set_apply_form(0)
     return H.dv, Q
 
 
@@ -428,14 +445,17 @@ if torch is not None:
         """(lam, Q) = eigen-decomposition of SymTridiagonal(d, e) by the GB300 qr_algorithm!,
         differentiable: the backward is symeig_eig_adjoint_f64_dev.  lam is unsorted (as
         H.dv of the reference); Q is returned as a column-major view.  The counterpart of the
-        Julia ChainRulesCore rrule of the Julia binding."""
+        Julia ChainRulesCore rrule of the Julia binding.  apply(d, e[, chase_mode[, apply_form]]):
+        the forward solve's chase mode and apply form as for qr_algorithm_ (default: the
+        reference's sweep sequence, canonical apply); the backward does not depend on them."""
 
         @staticmethod
-        def forward(ctx, d, e):
+        def forward(ctx, d, e, chase_mode=0, apply_form=0):
             n = d.shape[0]
             dd, ee = d.detach().clone().contiguous(), e.detach().clone().contiguous()
             Q = torch.eye(n, dtype=torch.float64, device=d.device).T.contiguous().T
-            _, conv, _ = qr_algorithm_(SymTridiagonal(dd, ee), Q)
+            _, conv, _ = qr_algorithm_(SymTridiagonal(dd, ee), Q, chase_mode=int(chase_mode),
+                                       apply_form=int(apply_form))
             if not conv:
                 raise RuntimeError("qr_algorithm! did not converge")
             ctx.save_for_backward(dd, Q)
@@ -447,7 +467,7 @@ if torch is not None:
             if glam is None:
                 glam = torch.zeros_like(lam)
             gd, ge = eig_adjoint(lam, Q, glam.contiguous(), gQ)
-            return gd, ge
+            return gd, ge, None, None
 
     class TridiagEighBatched(torch.autograd.Function):
         """Batched TridiagEigh: d (B, n), e (B, n-1) -> lam (B, n), Q (B, n, n) (each Q[b]

@@ -10,6 +10,7 @@
 // status (pinned memory) to learn whether to apply, stop (converged) or give up (maxiter),
 // exactly the three exits of the reference.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <chrono>
@@ -81,6 +82,22 @@ struct symeig_context {
 };
 
 namespace {
+
+// NVTX range over a host scope (header-only NVTX 3: a no-op unless a profiler is attached).
+// The qr driver marks each flush's chase (the host waits for it inside the range, so the
+// range spans its device time) and each apply enqueue; the bulk entry points mark the call.
+struct NvtxRange {
+    bool open = true;
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { end(); }
+    void end()
+    {
+        if (open) nvtxRangePop();
+        open = false;
+    }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 int cuda_status(cudaError_t e)
 {
@@ -268,6 +285,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
         if (flush >= 1) CK(cudaStreamWaitEvent(cs, h->ev_consumed[b ^ 1], 0));
         cudaEvent_t c0 = timing_event(h, tev++), c1 = timing_event(h, tev++);
         if (!c0 || !c1) return SYMEIG_ERR_CUDA;
+        NvtxRange nv_chase("symeig chase");
         CK(cudaEventRecord(c0, cs));
         BulgeScratch* bsc = (BulgeScratch*)h->bulge.ptr;
         CK(launch_chase(dstate, d, e, (double*)h->grid[b].ptr, (int32_t*)h->thick[b].ptr,
@@ -291,6 +309,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
             CK(cudaEventRecord(h->ev_chased[b], cs));
             CK(cudaEventSynchronize(h->ev_chased[b]));
         }
+        nv_chase.end();
         float ms_chase = 0.f;
         CK(cudaEventElapsedTime(&ms_chase, c0, c1));
         chase_ms += ms_chase;
@@ -311,6 +330,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
             CK(cudaEventRecord(a0, ms));
             const int64_t c_lo = st.min_from - 1;          // 0-based first column touched
             const int64_t n_loc = st.max_to - c_lo;         // columns from..to of every sweep
+            NvtxRange nv("symeig apply flush");
             rc = apply_grid<double, T>(h, Q, ldq, m, (const double*)h->grid[b].ptr, rows,
                                        (const int32_t*)h->place[b].ptr, c_lo, n_loc,
                                        st.max_thickness, ms);
@@ -390,6 +410,7 @@ int qr_host(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq,
 template <typename T>
 int apply_dev(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T* cs, int64_t k)
 {
+    NvtxRange nv("symeig apply_givens (device pointers)");
     int rc = check_handle(h);
     if (rc) return rc;
     if (k < 0 || n < 0) return SYMEIG_ERR_SIZE;
@@ -466,6 +487,7 @@ int apply_host_pipelined(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t 
 template <typename T>
 int apply_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T* cs, int64_t k)
 {
+    NvtxRange nv("symeig apply_givens (host pointers)");
     int rc = check_handle(h);
     if (rc) return rc;
     if (k < 0 || n < 0) return SYMEIG_ERR_SIZE;
@@ -854,6 +876,7 @@ int symeig_qr_batched_f64_dev(symeig_handle h, int64_t count, const int64_t* n, 
                               double* e, double* Q, int32_t max_layers, double tol,
                               int64_t maxiter_factor, int32_t* converged, int64_t* iters)
 {
+    NvtxRange nv("symeig qr batched");
     int rc = check_handle(h);
     if (rc) return rc;
     if (count < 0) return SYMEIG_ERR_SIZE;
@@ -946,6 +969,7 @@ int symeig_eig_adjoint_f64_dev(symeig_handle h, int64_t count, int64_t n, const 
                                const double* Q, const double* glam, const double* gQ, double* gd,
                                double* ge)
 {
+    NvtxRange nv("symeig adjoint");
     int rc = check_handle(h);
     if (rc) return rc;
     if (count < 0 || n < 0 || (count > 0 && n > (1 << 20))) return SYMEIG_ERR_SIZE;

@@ -14,6 +14,13 @@
 // table and give wrong results; calls issued on one stream are ordered and safe.  The
 // table-build kernel rewrites every table entry a pass reads before the pass runs, so the
 // contents left by the previous call never need clearing.
+//
+// The calls are asynchronous, so a bounded wait that gave up inside a kernel (the error
+// word below) cannot change their return value.  symeig_noalloc_status reads and clears
+// that word after the caller's stream has drained.  Under lazy module loading (the CUDA
+// default) the array is claimed when this file's module first loads on a device, i.e. at
+// the first call there; symeig_noalloc_init does that step on its own, so a caller can run
+// it before its own allocator takes the device's memory and before any stream capture.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -25,7 +32,7 @@ namespace symeig {
 namespace {
 
 // The scratch: one pass's wave table, and the kernel's error word (set to 1 if a bounded
-// wait inside the kernel gave up; never cleared by the library).
+// wait inside the kernel gave up; read and cleared by symeig_noalloc_status).
 static __device__ __align__(256) unsigned char g_noalloc_table[SYMEIG_NOALLOC_SCRATCH_BYTES];
 static __device__ int g_noalloc_err;
 
@@ -56,6 +63,31 @@ int table_address(void** table, int** err)
 
 }  // namespace
 }  // namespace symeig
+
+extern "C" int symeig_noalloc_init(void)
+{
+    void* table = nullptr;
+    int* err = nullptr;
+    return symeig::table_address(&table, &err);
+}
+
+extern "C" int symeig_noalloc_status(void* stream)
+{
+    void* table = nullptr;
+    int* err = nullptr;
+    int rc = symeig::table_address(&table, &err);
+    if (rc) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    int word = 0;
+    if (cudaMemcpyAsync(&word, err, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess) return SYMEIG_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return SYMEIG_ERR_CUDA;
+    if (word != 0) {
+        if (cudaMemsetAsync(err, 0, sizeof(int), s) != cudaSuccess) return SYMEIG_ERR_CUDA;
+        if (cudaStreamSynchronize(s) != cudaSuccess) return SYMEIG_ERR_CUDA;
+        return SYMEIG_ERR_TIMEOUT;
+    }
+    return SYMEIG_OK;
+}
 
 extern "C" int symeig_apply_givens_f64_noalloc(double* A, int64_t lda, int64_t m, int64_t n,
                                                const double* cs, int64_t k, void* stream)

@@ -67,17 +67,26 @@ def test_oracle_eigenvalues_match_lapack(oracle, n, seed):
 
 
 def test_oracle_readme_example_n2000(oracle):
-    """README.md:65-77: n=2000, d=1:n, e=rand -> ||A Q - Q D|| = 2.86e-10 in the README.
-    Our seeded e gives the same magnitude; the flush count matches the reference's buffer
-    rule (18 flushes of at most 128 layers)."""
+    """README.md:65-77: n=2000, d=1:n, e=rand -> ||A Q - Q D||_F = 2.86e-10 in the README.
+    The reference's Julia RNG stream cannot be reproduced here, so e comes from numpy
+    (seed 0); the residual must then have the README's magnitude (within a factor 2), and
+    the solve must take the 18 flushes of at most 128 layers that the reference's buffer rule
+    gives for this matrix.  Eigenvalues within 10 n eps ||T|| of LAPACK."""
     n = 2000
     rng = np.random.default_rng(0)
     d, e = np.arange(1, n + 1, dtype=np.float64), rng.random(n - 1)
     dd, ee = d.copy(), e.copy()
-    conv, it, flushes, rot = oracle.qr_algorithm(dd, ee, None)
+    Q = np.asfortranarray(np.eye(n))
+    conv, it, flushes, rot = oracle.qr_algorithm(dd, ee, Q)
     assert conv
+    assert flushes == 18
+    T = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
+    resid = np.linalg.norm(T @ Q - Q * dd)
+    assert 2.86e-10 / 2 <= resid <= 2.86e-10 * 2, resid
     lam = eigh_tridiagonal(d, e, eigvals_only=True)
-    assert np.max(np.abs(np.sort(dd) - lam)) <= 10 * n * np.finfo(float).eps * n
+    eps = np.finfo(float).eps
+    assert np.max(np.abs(np.sort(dd) - lam)) <= 10 * n * eps * np.max(np.abs(lam))
+    assert np.linalg.norm(Q.T @ Q - np.eye(n)) <= 10 * n * eps
 
 
 def test_wave_order_port_equals_layer_major(pkg, oracle):
