@@ -298,6 +298,15 @@ int symeig_get_rotation_f64(symeig_handle h, int64_t count, const double* f, con
                             double* c, double* s, double* r);
 int symeig_get_rotation_f64_dev(symeig_handle h, int64_t count, const double* f, const double* g,
                                 double* c, double* s, double* r);
+/* Elementwise FP64 products out[i] = a[i] * b[i] of device arrays on the handle's stream:
+ * form 0 as the canonical bulk apply computes its rotation products (from integer
+ * arithmetic on GB300's integer pipes, bit for bit the IEEE round-to-nearest product; lanes
+ * with a zero, subnormal, infinite or NaN operand or an out-of-range result are recomputed on
+ * the FP64 pipe), form 1 with the FP64 multiply.  A self-check of the apply's arithmetic: both
+ * forms give the same bits.  No reference counterpart (the products are those of rmul!,
+ * src/simple_givens.jl:53-65). */
+int symeig_mul_rn_f64_dev(symeig_handle h, int64_t count, const double* a, const double* b, double* out,
+                          int32_t form);
 /* ---- eigen_decomp!  (src/bulge_chasing.jl:290-299) ----------------------------------- *
  * Q (n x n, ldq >= n) is set to the identity, then qr_algorithm! runs with the default
  * max_layers = 128, tol = eps, maxiter = 100n.  d/e overwritten as in symeig_qr_f64. */

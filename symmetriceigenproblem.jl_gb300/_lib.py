@@ -44,6 +44,7 @@ SIGNATURES = {
     "symeig_syev_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp]),
     "symeig_syev_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_i64, c_vp, c_vp, c_i64, c_vp, c_vp]),
     "symeig_get_rotation_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
+    "symeig_mul_rn_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_i32]),
     "symeig_set_kernel_timing": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_measure_fma_peak": (ctypes.c_int, [ctypes.c_int, c_i32, ctypes.POINTER(c_dbl)]),
     "symeig_measure_dmma_peak": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(c_dbl)]),

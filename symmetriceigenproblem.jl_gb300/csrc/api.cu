@@ -750,7 +750,7 @@ int symeig_set_multishift(symeig_handle h, int32_t max_bulges, int32_t rows_per_
 int symeig_set_apply_form(symeig_handle h, int32_t form)
 {
     if (!h) return SYMEIG_ERR_HANDLE;
-    if (form < 0 || form > 1) return SYMEIG_ERR_SIZE;
+    if (form < 0 || form > 2) return SYMEIG_ERR_SIZE;
     h->apply_form = form;
     return SYMEIG_OK;
 }
@@ -1145,6 +1145,18 @@ int symeig_get_rotation_f64_dev(symeig_handle h, int64_t count, const double* f,
     if (count > 0 && (!f || !g || !c || !s || !r)) return SYMEIG_ERR_NULL;
     begin_call(h);
     CK(launch_get_rotation(count, f, g, c, s, r, h->chase_mode == 1 ? 1 : 0, h->stream));
+    return SYMEIG_OK;
+}
+
+int symeig_mul_rn_f64_dev(symeig_handle h, int64_t count, const double* a, const double* b, double* out,
+                          int32_t form)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (count < 0 || form < 0 || form > 1) return SYMEIG_ERR_SIZE;
+    if (count > 0 && (!a || !b || !out)) return SYMEIG_ERR_NULL;
+    begin_call(h);
+    CK(launch_mul_rn(count, a, b, out, form, h->stream));
     return SYMEIG_OK;
 }
 

@@ -32,16 +32,18 @@ using wave::kThreads;
 //             rotation-row, and each thread has two independent rotation chains.  Shape 2
 //             is the FP32 choice (1.5-3 % ahead of shape 1, measured).
 template <typename T, int S> struct Cfg;
-template <> struct Cfg<double, 0> { using Sh = Shape<double, 8, 8>; static constexpr int MINB = 7; static constexpr int THREADS = Sh::THREADS; };
-template <> struct Cfg<double, 1> { using Sh = Shape<double, 16, 4>; static constexpr int MINB = 4; static constexpr int THREADS = Sh::THREADS; };
-template <> struct Cfg<float, 0> { using Sh = Shape<float, 8, 8>; static constexpr int MINB = 7; static constexpr int THREADS = Sh::THREADS; };
-template <> struct Cfg<float, 1> { using Sh = Shape<float, 16, 4>; static constexpr int MINB = 5; static constexpr int THREADS = Sh::THREADS; };
-template <> struct Cfg<float, 2> { using Sh = Shape<float, 16, 4, 2>; static constexpr int MINB = 3; static constexpr int THREADS = Sh::THREADS; };
+// MINB: CTAs per SM the launch bounds ask for; MINB_INT the same for the FP64 kernels whose
+// products run on the integer pipes (int_mul.cuh: about 95 registers with one row per thread).
+template <> struct Cfg<double, 0> { using Sh = Shape<double, 8, 8>; static constexpr int MINB = 7, MINB_INT = 5; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<double, 1> { using Sh = Shape<double, 16, 4>; static constexpr int MINB = 4, MINB_INT = 3; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<float, 0> { using Sh = Shape<float, 8, 8>; static constexpr int MINB = 7, MINB_INT = 7; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<float, 1> { using Sh = Shape<float, 16, 4>; static constexpr int MINB = 5, MINB_INT = 5; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<float, 2> { using Sh = Shape<float, 16, 4, 2>; static constexpr int MINB = 3, MINB_INT = 3; static constexpr int THREADS = Sh::THREADS; };
 // FP64 shape 2 = shape 0 in one CTA of 27 warps (108 rows): at m = 16384 that is 152 CTAs, one
 // per SM, every SM with the same rows, where 1024 CTAs of 16 rows leave 112 SMs with 7 CTAs and
 // 40 with 6 (the kernel's time is the busiest SM's).  27 warps x 72 registers fit one SM.
-template <> struct Cfg<double, 2> { using Sh = Shape<double, 8, 8, 1, 27>; static constexpr int MINB = 1; static constexpr int THREADS = Sh::THREADS; };
-template <> struct Cfg<float, 3> { using Sh = Shape<float, 8, 8, 2>; static constexpr int MINB = 4; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<double, 2> { using Sh = Shape<double, 8, 8, 1, 27>; static constexpr int MINB = 1, MINB_INT = 1; static constexpr int THREADS = Sh::THREADS; };
+template <> struct Cfg<float, 3> { using Sh = Shape<float, 8, 8, 2>; static constexpr int MINB = 4, MINB_INT = 4; static constexpr int THREADS = Sh::THREADS; };
 // the table depends on (KB, G) only, so shapes 2 and 3 share the tables of 1 and 0
 static_assert(Cfg<float, 2>::Sh::CHUNK == Cfg<float, 1>::Sh::CHUNK, "table layout");
 static_assert(Cfg<float, 3>::Sh::CHUNK == Cfg<float, 0>::Sh::CHUNK, "table layout");
@@ -50,6 +52,11 @@ static_assert(Cfg<double, 2>::Sh::CHUNK == Cfg<double, 0>::Sh::CHUNK, "table lay
 constexpr int kShapes[2] = {3, 4};  // shapes available to [0] FP64, [1] FP32
 // FP64 shape 0 runs as shape 2 from this many rows on (about 152 SMs x 108 rows x 0.92)
 constexpr int64_t kWideRows = 15000;
+// The canonical FP64 form computes its products on the integer pipes from this many rows on.
+// Below it the grid has too few warps to hide the integer products' longer dependency chain
+// (measured, 64 layers on m x m: 556 against 642 GFLOP/s at m = 2000, 916 against 710 at
+// m = 4096), and the products stay on the FP64 pipe; both give the same bits.
+constexpr int64_t kIntMulRows = 3072;
 int g_shape[2] = {0, 2};            // [0] FP64, [1] FP32
 template <typename T> int shape_index() { return g_shape[sizeof(T) == 8 ? 0 : 1]; }
 
@@ -291,8 +298,8 @@ scaled_table_kernel(unsigned char* __restrict__ table, int64_t n_chunks, const T
     }
 }
 
-template <typename T, int S, bool SCALED = false>
-__global__ void __launch_bounds__(Cfg<T, S>::THREADS, Cfg<T, S>::MINB)
+template <typename T, int S, bool SCALED = false, bool INT_MUL = false>
+__global__ void __launch_bounds__(Cfg<T, S>::THREADS, INT_MUL ? Cfg<T, S>::MINB_INT : Cfg<T, S>::MINB)
 wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
                   const unsigned char* __restrict__ table, int32_t n_chunks, int* __restrict__ err,
                   const T nz, int64_t rs, int32_t stall)
@@ -303,12 +310,50 @@ wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
     wave::Staging<Sh> st{ring, bar, 0, 0};
     wave::staging_init(st);
     const int64_t row0 = (int64_t)blockIdx.x * Sh::ROWS;
-    if (!wave::wave_tile<T, Sh, SCALED>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs, stall)) {
+    if (!wave::wave_tile<T, Sh, SCALED, INT_MUL>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs, stall)) {
         if (threadIdx.x == 0) atomicExch(err, 1);
     }
 }
 
+// Elementwise products a[i] * b[i]: form 0 as the canonical FP64 apply computes them
+// (integer pipes, FP64-pipe recomputation of the lanes the integer path does not cover),
+// form 1 on the FP64 pipe.  A self-check of int_mul.cuh against the FP64 multiply.
+__global__ void __launch_bounds__(256)
+mul_rn_kernel(int64_t count, const double* __restrict__ a, const double* __restrict__ b,
+              double* __restrict__ out, int32_t form, double nz)
+{
+    // every lane of a warp runs the same number of loop trips (the vote inside needs them all)
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t base = (int64_t)blockIdx.x * blockDim.x;
+    for (int64_t i0 = base; i0 < count; i0 += stride) {
+        const int64_t i = i0 + threadIdx.x;
+        const bool ok = i < count;
+        const double x = ok ? a[i] : 1.0, y = ok ? b[i] : 1.0;
+        double p;
+        if (form == 0) {
+            const SplitFactor f = split_factor(x);
+            bool sp = f.special;
+            p = mul_rn_int(f, y, sp);
+            if (__any_sync(0xffffffffu, sp)) {
+                if (sp) p = fma_pair_call(x, y, y, nz).x;
+            }
+        } else {
+            p = __dmul_rn(x, y);
+        }
+        if (ok) out[i] = p;
+    }
+}
+
 }  // namespace
+
+cudaError_t launch_mul_rn(int64_t count, const double* a, const double* b, double* out, int32_t form,
+                          cudaStream_t stream)
+{
+    if (count <= 0) return cudaSuccess;
+    const int64_t blocks = (count + 255) / 256 < 1216 ? (count + 255) / 256 : 1216;
+    mul_rn_kernel<<<(unsigned)blocks, 256, 0, stream>>>(count, a, b, out, form, -0.0);
+    return cudaGetLastError();
+}
 
 template <typename T> int64_t apply_layers_per_pass() { return 64; }
 template int64_t apply_layers_per_pass<double>();
@@ -414,9 +459,18 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
     }
     if (!run) return cudaSuccess;
     if (ev_begin) cudaEventRecord(ev_begin, stream);
-    wave_apply_kernel<T, S><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
-        Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
-        (int32_t)n_chunks, err, (T)-0.0, pass.rs, pass.stall > 0 ? pass.stall : 0x7fffffff);
+    bool int_mul = false;
+    if constexpr (sizeof(T) == 8) {
+        int_mul = pass.form == 0 && m >= kIntMulRows;   // canonical FP64: products on the integer pipes
+        if (int_mul)
+            wave_apply_kernel<T, S, false, true><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
+                Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
+                (int32_t)n_chunks, err, (T)-0.0, pass.rs, pass.stall > 0 ? pass.stall : 0x7fffffff);
+    }
+    if (!int_mul)
+        wave_apply_kernel<T, S><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
+            Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
+            (int32_t)n_chunks, err, (T)-0.0, pass.rs, pass.stall > 0 ? pass.stall : 0x7fffffff);
     e = cudaGetLastError();
     if (ev_end) cudaEventRecord(ev_end, stream);
     return e;

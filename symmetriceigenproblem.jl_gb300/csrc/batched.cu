@@ -203,8 +203,9 @@ batched_wave_kernel(const BatchMat* __restrict__ mats, const Work* __restrict__ 
         const Work w = work[lo];
         const int64_t row0 = (tile - prefix[lo]) * Sh::ROWS;
         double* q = Q + mt.qoff + w.c0 * mt.n;
-        if (!wave::wave_tile<double, Sh>(q, mt.n, mt.n, row0, (int32_t)w.n_loc, tables + toff[lo],
-                                         (int32_t)Sh::chunks(w.n_loc), nz, st)) {
+        // the canonical rotation with its products on the integer pipes (int_mul.cuh)
+        if (!wave::wave_tile<double, Sh, false, true>(q, mt.n, mt.n, row0, (int32_t)w.n_loc, tables + toff[lo],
+                                                      (int32_t)Sh::chunks(w.n_loc), nz, st)) {
             if (threadIdx.x == 0) atomicExch(err, 1);
             return;
         }

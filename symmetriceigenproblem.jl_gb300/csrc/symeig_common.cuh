@@ -175,6 +175,9 @@ cudaError_t launch_dense_scale(double* A, int64_t lda, int64_t n, double scale, 
 // d *= f, e *= f, and the diagonal / subdiagonal of A set from them
 cudaError_t launch_tridiag_unscale(double* A, int64_t lda, int64_t n, double* d, double* e,
                                    double f, cudaStream_t s);
+// a[i] * b[i] elementwise: form 0 the canonical apply's integer-pipe products, 1 the FP64 pipe.
+cudaError_t launch_mul_rn(int64_t count, const double* a, const double* b, double* out, int32_t form,
+                          cudaStream_t stream);
 // givensAlgorithm elementwise on device arrays (form 0 Newton form, 1 reference form).
 cudaError_t launch_get_rotation(int64_t count, const double* f, const double* g, double* c,
                                 double* s, double* r, int32_t form, cudaStream_t stream);

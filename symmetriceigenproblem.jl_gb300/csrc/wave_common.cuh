@@ -37,6 +37,7 @@
 // columns of Q, read KB+1 waves ahead.
 #pragma once
 
+#include "int_mul.cuh"
 #include "symeig_common.cuh"
 
 namespace symeig {
@@ -149,13 +150,40 @@ __device__ __forceinline__ void table_entry(unsigned char* table, int64_t t, int
 // The KB rotations of one wave on the windows of the thread's R rows, (c,s) read from shared
 // memory once for all R rows.  U is the wave's slot (t mod (KB+1)); callers pass a constant of
 // a fully unrolled loop, so every window index folds to a constant and the windows stay in
-// registers.
-template <typename T, int KB, int R>
+// registers.  FP64 with INT_MUL: the products s*y and s*x of each rotation come from the
+// integer pipes (int_mul.cuh), bit-identical to the FP64 products, and only the two FMAs use
+// the FP64 pipe; a lane whose product the integer path does not cover (a zero, subnormal,
+// infinite or NaN operand, an underflow) recomputes both products on the FP64 pipe, behind a
+// warp vote so that the FP64 instructions issue only when some lane needs them.
+template <typename T, int KB, int R, bool INT_MUL = false>
 __device__ __forceinline__ void wave_rotations(T (&win)[R][KB + 1], const unsigned char* cs, const int U,
                                                const T nz)
 {
     constexpr int W = KB + 1;
-    if constexpr (sizeof(T) == 8) {
+    if constexpr (sizeof(T) == 8 && INT_MUL) {
+#pragma unroll
+        for (int l = 0; l < KB; ++l) {
+            const double2 p = *reinterpret_cast<const double2*>(cs + l * 16);
+            const SplitFactor f = split_factor(p.y);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                double& x = win[r][(U - 1 - l + 2 * W) % W];
+                double& y = win[r][(U - l + 2 * W) % W];
+                bool sp = f.special;
+                double sy = mul_rn_int(f, y, sp);
+                double sx = mul_rn_int(f, x, sp);
+                if (__any_sync(0xffffffffu, sp)) {
+                    if (sp) {
+                        const double2 q = fma_pair_call(p.y, y, x, nz);
+                        sy = q.x;
+                        sx = q.y;
+                    }
+                }
+                x = __fma_rn(p.x, x, sy);
+                y = __fma_rn(p.x, y, -sx);
+            }
+        }
+    } else if constexpr (sizeof(T) == 8) {
 #pragma unroll
         for (int l = 0; l < KB; ++l) {
             const double2 p = *reinterpret_cast<const double2*>(cs + l * 16);
@@ -231,7 +259,7 @@ __device__ __forceinline__ void staging_init(Staging<Sh>& st)
 // the column rotations of rmul! on a column-major matrix, rs = lda and ldq = 1 for the row
 // rotations of lmul! (the same wave on the transposed view).  Every thread of the CTA calls
 // it.  Returns false (all threads) when a bounded wait gave up.
-template <typename T, typename Sh, bool SCALED = false>
+template <typename T, typename Sh, bool SCALED = false, bool INT_MUL = false>
 __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_t m, int64_t row0,
                                           int32_t n_loc, const unsigned char* __restrict__ table,
                                           int32_t n_chunks, const T nz, Staging<Sh>& st,
@@ -304,7 +332,7 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
                     win[r][u % W] = xin;
                 }
                 if constexpr (SCALED) wave_rotations_scaled<KB, R>(win, sb + u * Sh::ITER, u % W);
-                else wave_rotations<T, KB, R>(win, sb + u * Sh::ITER, u % W, nz);
+                else wave_rotations<T, KB, R, INT_MUL>(win, sb + u * Sh::ITER, u % W, nz);
                 T dsc = T(1);
                 if constexpr (SCALED) dsc = *reinterpret_cast<const T*>(sb + u * Sh::ITER + KB * 16 + 8);
 #pragma unroll
@@ -334,7 +362,7 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
                     win[r][u % W] = xin;
                 }
                 if constexpr (SCALED) wave_rotations_scaled<KB, R>(win, sb + u * Sh::ITER, u % W);
-                else wave_rotations<T, KB, R>(win, sb + u * Sh::ITER, u % W, nz);
+                else wave_rotations<T, KB, R, INT_MUL>(win, sb + u * Sh::ITER, u % W, nz);
                 T dsc = T(1);
                 if constexpr (SCALED) dsc = *reinterpret_cast<const T*>(sb + u * Sh::ITER + KB * 16 + 8);
 #pragma unroll
