@@ -14,6 +14,17 @@ replica on its own GPU (the path does not shard; the reference's row slabs would
 broadcast of (c,s)), and `value` sums the replicas' work over the slowest rank's time.
 `--impl reference` times the CPU restatement of the reference's wave kernel
 (oracle/symeig_oracle.c, row-slab threaded like src/wave.jl:36-60) on all host cores.
+
+The default line also carries, untimed by `value`, the other items of the metric:
+  solve_n16384          qr_algorithm! at n = 16384 (case A) on the device, multishift chase,
+                        with its errors, beside cpu_reference_solve_n16384, the reference's own
+                        solve path (its chase, then every flush's grid by the row-slab threaded
+                        wave kernel) timed on the host cores on a row sample of Q;
+  solve_n2000[_multishift]  the README example (README.md:65-77);
+  batched               4096 tridiagonals n ~ U{32..1024}: batched call vs a loop of single
+                        solves on the batch's own matrices vs the host;
+  adjoint               n = 4096 forward + backward / forward, with the gradient's error;
+  f32_apply, scaled_form    the FP32 apply and the scaled FP64 form on the apply workload.
 """
 from __future__ import annotations
 
@@ -47,7 +58,9 @@ def parse_args():
     p.add_argument("--m", type=int, default=16384)
     p.add_argument("--n", type=int, default=16384)
     p.add_argument("--k", type=int, default=64)
-    p.add_argument("--no-extras", action="store_true", help="skip the FP32 and n=2000 side measurements")
+    p.add_argument("--no-extras", action="store_true", help="skip every side measurement of the default line")
+    p.add_argument("--no-solve-extras", action="store_true",
+                   help="skip the n=16384 solve, batched and adjoint keys of the default line")
     p.add_argument("--workload", choices=["apply", "solve", "batched", "adjoint", "dense"], default="apply",
                    help="apply: the bulk-apply microbenchmark (default); solve: one full qr_algorithm!")
     p.add_argument("--case", choices=["A", "B"], default="A",
@@ -58,9 +71,9 @@ def parse_args():
     p.add_argument("--form", choices=["canonical", "scaled"], default="canonical",
                    help="FP64 apply form: canonical rotations (4 FP64 ops per rotation-row) or the "
                         "scaled form (2 FMAs per rotation-row; a few ulps from canonical)")
-    p.add_argument("--chase-mode", type=int, choices=[0, 1, 2, 3], default=0,
-                   help="solve workload: 0 Newton-form two-warp chase, 1 reference form, 2 Newton + redo, "
-                        "3 multishift batches")
+    p.add_argument("--chase-mode", type=int, choices=[0, 1, 2, 3], default=None,
+                   help="solve/dense workloads (default 0) and the adjoint's forward (default 3): 0 Newton-form "
+                        "two-warp chase, 1 reference form, 2 Newton + redo, 3 multishift batches")
     p.add_argument("--ms-bulges", type=int, default=64, help="solve workload, chase mode 3: bulge cap of a batch")
     p.add_argument("--ms-rows", type=int, default=16, help="solve workload, chase mode 3: block rows per bulge")
     p.add_argument("--ms-release", type=int, default=4, help="solve workload, chase mode 3: steps between progress releases")
@@ -142,9 +155,10 @@ class ClockSampler:
 
 # ---- CPU side (the oracle's port of the reference's wave kernel) ---------------------------
 def cpu_wave_gflops(m, n, k, dtype, threads, target_s=8.0, max_rows=None):
-    """Time the reference's wave-order kernel (C port, row slabs on `threads` threads) on a
-    bounded row sample of the workload; GFLOP/s scales with rows, so the sample is
-    representative.  Returns (gflops, rows, seconds)."""
+    """Time the reference's wave-order kernel (C port, row slabs on `threads` threads, the
+    timing build: contraction allowed and tuned for the host's cores) on a bounded row sample of
+    the workload; GFLOP/s scales with rows, so the sample is representative.  Returns
+    (gflops, rows, seconds, shape)."""
     from oracle import oracle as orc
     orc.build()
     rng = np.random.default_rng(1)
@@ -160,12 +174,61 @@ def cpu_wave_gflops(m, n, k, dtype, threads, target_s=8.0, max_rows=None):
     while True:
         Q = np.asfortranarray(rng.random((rows, nn)).astype(npdt) * 2 - 1)
         t0 = time.perf_counter()
-        orc.apply_wave(Q, cs, nthreads=threads)
+        orc.apply_wave(Q, cs, nthreads=threads, fast=True)
         dt = time.perf_counter() - t0
         cap = max_rows or m
         if dt >= target_s * 0.5 or rows >= cap:
             return flops_per_step(rows, nn, kk) / dt / 1e9, rows, dt, (rows, nn, kk)
         rows = int(min(cap, rows * max(2.0, min(16.0, target_s / max(dt, 1e-3)))))
+
+
+_HOST_PEAK_SCRIPT = """
+import json, time, numpy as np
+n = 4096
+a = np.random.default_rng(0).random((n, n)); b = np.random.default_rng(1).random((n, n))
+a @ b
+best = 1e30
+for _ in range(3):
+    t0 = time.perf_counter(); a @ b; best = min(best, time.perf_counter() - t0)
+print(json.dumps(2.0 * n ** 3 / best / 1e9))
+"""
+
+
+def host_peak(threads):
+    """DGEMM rate of the host (numpy's BLAS, n = 4096, best of 3) on one thread -- the
+    analogue of the reference's single-threaded LinearAlgebra.peakflops() (README.md:28-34) --
+    and on `threads` threads.  Each in a subprocess with the BLAS thread count fixed at start."""
+    out = {"n": 4096, "kind": "numpy BLAS dgemm, best of 3"}
+    for key, t in (("one_thread_gflops", 1), ("all_threads_gflops", threads)):
+        env = dict(os.environ, OPENBLAS_NUM_THREADS=str(t), OMP_NUM_THREADS=str(t), MKL_NUM_THREADS=str(t))
+        try:
+            r = subprocess.run([sys.executable, "-c", _HOST_PEAK_SCRIPT], env=env, capture_output=True,
+                               text=True, timeout=300)
+            out[key] = round(float(r.stdout.strip().splitlines()[-1]), 2)
+        except Exception as exc:  # reported, not fatal: the baseline stands without it
+            out[key] = None
+            out["error"] = f"{type(exc).__name__}"
+    return out
+
+
+def cpu_baseline_apply(m, n, k, dtype, threads):
+    """The cpu_baseline object of the apply workload: the C port of the reference's wave
+    kernel on all host cores and on one, with the host's DGEMM rates beside it."""
+    gf, rows, dt, shape = cpu_wave_gflops(m, n, k, dtype, threads, target_s=8.0)
+    cpu = {"value": round(gf, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
+           "sample": (f"C port of the reference wave kernel (timing build), {threads} threads, {shape[0]} of {m} "
+                      f"rows x {shape[1]} cols, k={shape[2]}, {dt:.1f} s")}
+    gf1, _, dt1, shape1 = cpu_wave_gflops(m, n, k, dtype, 1, target_s=3.0, max_rows=1024)
+    cpu["one_thread"] = {"value": round(gf1, 3), "unit": "GFLOP/s", "cores": 1,
+                         "sample": f"{shape1[0]} of {m} rows x {shape1[1]} cols, k={shape1[2]}, {dt1:.1f} s"}
+    hp = host_peak(threads)
+    cpu["host_peak"] = hp
+    if dtype == "f64" and hp.get("one_thread_gflops"):
+        # the reference reports its kernel at 75% of single-thread dgemm (README.md:34)
+        cpu["frac_of_host_peak"] = {"one_thread": round(gf1 / hp["one_thread_gflops"], 4)}
+        if hp.get("all_threads_gflops"):
+            cpu["frac_of_host_peak"]["all_threads"] = round(gf / hp["all_threads_gflops"], 4)
+    return cpu
 
 
 def replica_reduce(ms: float, world: int, device=None) -> float:
@@ -200,7 +263,7 @@ def run_reference(args):
             vals.append((gf, dt))
     v = statistics.median([x[0] for x in vals])
     ms = statistics.median([x[1] for x in vals]) * 1e3
-    desc = (f"C port of the reference's wave kernel (oracle/symeig_oracle.c), {threads} threads, "
+    desc = (f"C port of the reference's wave kernel (oracle/symeig_oracle.c, timing build), {threads} threads, "
             f"row sample {sample[0]} of {args.m} rows x {sample[1]} cols, k={sample[2]}")
     line = {
         "metric": METRIC, "value": round(v, 3), "unit": "GFLOP/s", "impl": "reference",
@@ -210,7 +273,7 @@ def run_reference(args):
         "config": {"workload": WORKLOAD, "m": args.m, "n": args.n, "k": args.k, "parallelism": "cpu threads",
                    "l2": "n/a (CPU)"},
         "cpu_baseline": {"value": round(v, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
-                         "sample": desc},
+                         "sample": desc, "host_peak": host_peak(threads)},
         "e2e": {"value": round(v, 3), "unit": "GFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -303,8 +366,11 @@ def run_ours(args):
     fl = flops_per_step(m, n, k)
     value = replica_value(fl, world, ms_per_step) / 1e9
 
-    # roofline of the dominant kernel: the FP64 (FP32) FMA pipe
+    # roofline of the dominant kernel: the FP64 (FP32) FMA pipe.  The canonical FP64 form
+    # computes its products on the integer pipes from 3072 rows on (csrc/apply.cu)
     peak = pkg._lib.measure_fma_peak(local, fp64=(args.dtype == "f64"))
+    int_mul = args.dtype == "f64" and form == 0 and m >= 3072
+    pipe_ops = 2 if (form == 1 or int_mul) else 4
     per_launch_ms = statistics.median(kernel_ms)
     passes = max(1, -(-k // 64))
     achieved = fl / passes / (per_launch_ms * 1e-3) / 1e12
@@ -345,15 +411,7 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        gf, rows, dt, shape = cpu_wave_gflops(m, n, k, args.dtype, threads, target_s=8.0)
-        cpu = {"value": round(gf, 3), "unit": "GFLOP/s", "cores": threads, "kind": "port",
-               "sample": (f"C port of the reference wave kernel, {threads} threads, {shape[0]} of {m} rows "
-                          f"x {shape[1]} cols, k={shape[2]}, {dt:.1f} s")}
-        # the same kernel on one thread (a bounded row sample)
-        gf1, _, dt1, shape1 = cpu_wave_gflops(m, n, k, args.dtype, 1, target_s=3.0, max_rows=1024)
-        cpu["one_thread"] = {"value": round(gf1, 3), "unit": "GFLOP/s", "cores": 1,
-                             "sample": f"{shape1[0]} of {m} rows x {shape1[1]} cols, k={shape1[2]}, {dt1:.1f} s"}
+        cpu = cpu_baseline_apply(m, n, k, args.dtype, os.cpu_count() or 1)
 
     if rank == 0:
         line = {
@@ -368,14 +426,19 @@ def run_ours(args):
                        "l2": "inputs larger than L2 (Q = %.2f GB)" % (m * n * esz / 1e9)},
             "roofline": {"bound": "fp64" if args.dtype == "f64" else "fp32", "achieved": round(achieved, 4),
                          "peak": round(peak, 4), "unit": "TFLOP/s", "frac": round(achieved / peak, 4),
-                         "frac_of_givens_ceiling": round(achieved / peak / 0.75, 4),
-                         "peak_source": "measured now by symeig_measure_fma_peak (FMA = 2 flops); "
-                                        "a Givens rotation-row is 4 FMA-pipe ops for 6 counted flops, so 0.75 is the ceiling"
-                                        + ("; the scaled form spends 2 FMAs per rotation-row, so its ceiling is 1.5 and "
-                                           "fp64_pipe_frac is the measure of pipe use" if form else ""),
+                         "frac_of_givens_ceiling": round(achieved / peak / (6.0 / (2.0 * pipe_ops)), 4),
+                         "peak_source": "measured now by symeig_measure_fma_peak (FMA = 2 flops). " + (
+                             "A rotation-row is 6 counted flops: its two products run on the integer pipes "
+                             "(exact IEEE products, int_mul.cuh) and its two FMAs on the FP64 pipe, so the "
+                             "FP64-pipe ceiling is 6 / (2 x 2) = 1.5 of the FMA peak; fp64_pipe_frac is the "
+                             "pipe's use" if int_mul else
+                             "The scaled form spends 2 FMAs per rotation-row, so its ceiling is 1.5 and "
+                             "fp64_pipe_frac is the measure of pipe use" if form == 1 else
+                             "A Givens rotation-row is 4 FMA-pipe ops for 6 counted flops, so 0.75 is the ceiling"),
                          "hbm": hbm_side(algo_bytes, fl / passes, per_launch_ms, peak),
-                         "fp64_instr_per_rotation_row": 2 if form else 4,
-                         "fp64_pipe_frac": round((2 if form else 4) * (fl / 6.0 / passes) / (per_launch_ms * 1e-3)
+                         "fp64_instr_per_rotation_row": pipe_ops,
+                         "products_on_integer_pipes": int_mul,
+                         "fp64_pipe_frac": round(pipe_ops * (fl / 6.0 / passes) / (per_launch_ms * 1e-3)
                                                  / (peak * 1e12 / 2.0), 4),
                          "traffic": read_traffic(), "algorithmic_bytes": algo_bytes,
                          "kernel_ms": round(per_launch_ms, 3)},
@@ -471,6 +534,18 @@ def side_measurements(pkg, lib, h, dev, stream, args):
                                      "chase_ms": round(st["chase_ms"], 1), "apply_ms": round(st["apply_ms"], 1),
                                      "rotations": st["rotations"], "bulge_batches": st["bulge_batches"],
                                      "resid_rel": resid, "orth": orth, "bound_10n_eps": 10 * nn * 2.220446049250313e-16}
+    if args.no_solve_extras:
+        return out
+    # the full eigensolve at n = 16384 (case A) with the multishift chase, beside the
+    # reference's own solve path timed on the host cores
+    torch.cuda.synchronize()
+    out["solve_n16384"] = measure_solve(pkg, 16384, "A", "f64", 3, "canonical", with_clocks=False)
+    if not args.no_cpu_baseline:
+        out["cpu_reference_solve_n16384"] = cpu_reference_solve(16384, "A", os.cpu_count() or 1)
+        out["solve_n16384"]["speedup_vs_cpu_reference"] = round(
+            out["cpu_reference_solve_n16384"]["value"] / out["solve_n16384"]["seconds"], 2)
+    out["batched"] = measure_batched(pkg, with_cpu=not args.no_cpu_baseline)
+    out["adjoint"] = measure_adjoint(pkg, with_cpu=not args.no_cpu_baseline)
     return out
 
 
@@ -482,209 +557,266 @@ def solve_inputs(n, case):
     return rng.standard_normal(n), 0.5 * rng.standard_normal(n - 1)
 
 
-def run_solve(args):
-    """One full qr_algorithm!(SymTridiagonal(d, e), Q = I) on the device (the full-eigensolve
-    workload: n = 16384, case A or B, FP64 or FP32 Q), with its errors stated: eigenvalues
-    against LAPACK (scipy stemr) and, optionally, bit-for-bit against the CPU oracle's chase;
-    ||TQ - QD||_F / ||T||_F and ||Q^T Q - I||_F computed on the GPU in FP64."""
+def _tq_errors(torch, d, e, lam, Q):
+    """||TQ - Q diag(lam)||_F / ||T||_F and ||Q^T Q - I||_F in FP64 on the GPU (d, e: device
+    FP64 vectors; Q: device matrix, any float dtype)."""
+    Q = Q.to(torch.float64)
+    TQ = d[:, None] * Q
+    TQ[:-1] += e[:, None] * Q[1:]
+    TQ[1:] += e[:, None] * Q[:-1]
+    normT = math.sqrt(float((d * d).sum() + 2 * (e * e).sum()))
+    resid = float(torch.linalg.norm(TQ - Q * lam[None, :])) / normT
+    del TQ
+    G = Q.T @ Q
+    G.diagonal().sub_(1.0)
+    return resid, float(torch.linalg.norm(G))
+
+
+def measure_solve(pkg, n, case, q="f64", chase_mode=3, form="canonical", ms=(64, 16, 4), with_clocks=True):
+    """One full qr_algorithm!(SymTridiagonal(d, e), Q = I) on the device, with its errors:
+    eigenvalues against LAPACK (scipy stemr, host), ||TQ - QD||_F / ||T||_F and ||Q^T Q - I||_F
+    on the GPU in FP64."""
     import torch
-    import __graft_entry__ as ge
     from scipy.linalg import eigh_tridiagonal
-    pkg = ge.load_package()
-    n = args.n
-    d, e = solve_inputs(n, args.case)
-    torch.cuda.set_device(0)
+    d, e = solve_inputs(n, case)
     dev = torch.device("cuda", 0)
-    qdt = torch.float64 if args.q == "f64" else torch.float32
+    qdt = torch.float64 if q == "f64" else torch.float32
     h = pkg.Handle(0)
-    h.set_multishift(args.ms_bulges, args.ms_rows, args.ms_release)
+    h.set_multishift(*ms)
     td, te = torch.from_numpy(d.copy()).to(dev), torch.from_numpy(e.copy()).to(dev)
     Q = torch.eye(n, dtype=qdt, device=dev).T
     torch.cuda.synchronize()
-    with ClockSampler(0) as clk:
-        t0 = time.perf_counter()
-        _, conv, it = pkg.qr_algorithm_(pkg.SymTridiagonal(td, te), Q, handle=h, chase_mode=args.chase_mode,
-                                        apply_form=1 if (args.form == "scaled" and args.q == "f64") else 0)
-        torch.cuda.synchronize()
-        secs = time.perf_counter() - t0
+    clk = ClockSampler(0) if with_clocks else None
+    if clk:
+        clk.__enter__()
+    t0 = time.perf_counter()
+    _, conv, it = pkg.qr_algorithm_(pkg.SymTridiagonal(td, te), Q, handle=h, chase_mode=chase_mode,
+                                    apply_form=1 if (form == "scaled" and q == "f64") else 0)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    if clk:
+        clk.__exit__(None, None, None)
     st = h.stats()
+    h.close()
     lam = td.cpu().numpy()
-    # errors in FP64 on the GPU: T Q via the tridiagonal product, Q^T Q - I by GEMM
-    Q64 = Q.to(torch.float64)
-    dT, eT = torch.from_numpy(d).to(dev), torch.from_numpy(e).to(dev)
-    TQ = dT[:, None] * Q64
-    TQ[:-1] += eT[:, None] * Q64[1:]
-    TQ[1:] += eT[:, None] * Q64[:-1]
-    resid = float(torch.linalg.norm(TQ - Q64 * td[None, :]) / math.sqrt(float((d * d).sum() + 2 * (e * e).sum())))
-    del TQ
-    G = Q64.T @ Q64
-    G.diagonal().sub_(1.0)
-    orth = float(torch.linalg.norm(G))
-    del G, Q64
+    resid, orth = _tq_errors(torch, torch.from_numpy(d).to(dev), torch.from_numpy(e).to(dev), td, Q)
+    del Q
     t_lapack = time.perf_counter()
     ref = eigh_tridiagonal(d, e, eigvals_only=True)
     t_lapack = time.perf_counter() - t_lapack
     normT = float(np.max(np.abs(ref)))
     eig_err = float(np.max(np.abs(np.sort(lam) - ref)))
     eps = float(np.finfo(np.float64).eps)
+    out = {"seconds": round(secs, 3), "n": n, "case": case, "q": q, "chase_mode": chase_mode, "form": form,
+           "converged": bool(conv), "iterations": it, "rotations": st["rotations"], "flushes": st["flushes"],
+           "chase_ms": round(st["chase_ms"], 1), "apply_ms": round(st["apply_ms"], 1),
+           "givens_gflops_apply": round(6.0 * n * st["rotations"] / max(st["apply_ms"] * 1e-3, 1e-9) / 1e9, 1),
+           "applied_rotation_rows": st["applied_rotation_rows"], "bulge_batches": st["bulge_batches"],
+           "early_flushes": st["early_flushes"], "redone_sweeps": st["redone_sweeps"],
+           "errors": {"eig_max_abs_vs_lapack": eig_err, "eig_bound_10n_eps_normT": 10 * n * eps * normT,
+                      "resid_rel": resid, "orth": orth, "bound_10n_eps": 10 * n * eps,
+                      "eig_over_bound": eig_err / (10 * n * eps * normT), "resid_over_bound": resid / (10 * n * eps),
+                      "orth_over_bound": orth / (10 * n * eps)},
+           "lapack_eigvals": {"seconds": round(t_lapack, 3), "cores": os.cpu_count(),
+                              "kind": "scipy eigh_tridiagonal, eigenvalues only (no vectors), host"}}
+    if clk:
+        out["clocks"] = clk.summary()
+    return out
+
+
+def cpu_reference_solve(n, case, threads, apply_every=4):
+    """The reference's solve path timed on the host (oracle.qr_reference_path, timing build):
+    its chase on one core and its grid placement; after every flush, the whole (n-1) x 128 grid
+    applied to all n rows of Q by the row-slab threaded wave kernel on `threads` threads
+    (src/bulge_chasing.jl:146-288 -> src/wave.jl:36-60).  To bound the run, only every
+    apply_every-th flush is applied (the chase never reads Q, and the kernel's cost follows the
+    grid's rotations), and the apply time scales by rotations of all flushes / rotations of the
+    applied ones.  Even n only, as the reference."""
+    from oracle import oracle as orc
+    d, e = solve_inputs(n, case)
+    Q = np.asfortranarray(np.eye(n))
+    t0 = time.perf_counter()
+    conv, it, fl, tc, ta, ra, rt = orc.qr_reference_path(d, e, Q, max_layers=128, nthreads=threads, fast=True,
+                                                         apply_every=apply_every)
+    wall = time.perf_counter() - t0
+    scale = rt / max(ra, 1)
+    return {"value": round(tc + ta * scale, 2), "unit": "s", "cores": threads, "kind": "port",
+            "chase_s_1_core": round(tc, 3), "apply_s_sampled_flushes": round(ta, 3),
+            "apply_s_scaled": round(ta * scale, 2), "converged": conv, "iterations": it, "flushes": fl,
+            "rotations": rt, "rotations_of_applied_flushes": ra, "wall_s": round(wall, 2),
+            "sample": (f"the reference's solve path (oracle/symeig_oracle.c oracle_qr_reference_path, timing "
+                       f"build): chase on 1 core; every {apply_every}th flush's whole grid applied to all {n} "
+                       f"rows of Q by the row-slab wave kernel on {threads} threads; apply time scaled by "
+                       f"rotations, x{scale:.2f}")}
+
+
+def run_solve(args):
+    """One full qr_algorithm! on the device (the full-eigensolve workload: n = 16384, case A or
+    B, FP64 or FP32 Q), with its errors stated; --oracle-check adds the CPU oracle's chase
+    (bit-equal eigenvalues in chase modes 0-2) and the timed CPU baseline of the reference's
+    solve path."""
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    torch.cuda.set_device(0)
+    n = args.n
+    if args.chase_mode is None:
+        args.chase_mode = 0
+    r = measure_solve(pkg, n, args.case, args.q, args.chase_mode, args.form,
+                      (args.ms_bulges, args.ms_rows, args.ms_release))
     out = {
         "metric": f"qr_algorithm! full solve seconds, n={n} case {args.case}, Q {args.q}",
-        "value": round(secs, 3), "unit": "s", "higher_is_better": False, "n_gpus": 1,
+        "value": r["seconds"], "unit": "s", "higher_is_better": False, "n_gpus": 1,
         "dtype": "f64" if args.q == "f64" else "f64 chase, f32 Q",
         "data": "synthetic (seeded, as in the full-eigensolve configuration)",
         "config": {"workload": "qr_algorithm!(SymTridiagonal(d, e), Q = I)", "n": n, "case": args.case,
                    "q": args.q, "max_layers": 128, "chase_mode": args.chase_mode, "form": args.form,
                    **({"ms_bulges": args.ms_bulges, "ms_rows": args.ms_rows, "ms_release": args.ms_release}
                       if args.chase_mode == 3 else {})},
-        "converged": bool(conv), "iterations": it, "rotations": st["rotations"], "flushes": st["flushes"],
-        "chase_ms": round(st["chase_ms"], 1), "apply_ms": round(st["apply_ms"], 1),
-        "chase_us_per_rotation": round(st["chase_ms"] * 1e3 / max(st["rotations"], 1), 4),
-        "givens_gflops_apply": round(6.0 * n * st["rotations"] / (st["apply_ms"] * 1e-3) / 1e9, 1),
-        "early_flushes": st["early_flushes"], "redone_sweeps": st["redone_sweeps"],
-        "bulge_batches": st["bulge_batches"],
-        "errors": {"eig_max_abs_vs_lapack": eig_err, "eig_bound_10n_eps_normT": 10 * n * eps * normT,
-                   "resid_rel": resid, "orth": orth, "bound_10n_eps": 10 * n * eps},
-        "lapack_eigvals": {"seconds": round(t_lapack, 3), "cores": os.cpu_count(),
-                           "kind": "scipy eigh_tridiagonal, eigenvalues only (no vectors), host"},
-        "clocks": clk.summary(),
+        **{k: v for k, v in r.items() if k not in ("seconds",)},
     }
     if args.oracle_check:
         from oracle import oracle as orc
+        d, e = solve_inputs(n, args.case)
         od, oe = d.copy(), e.copy()
         t0 = time.perf_counter()
         c_o, it_o, fl_o, rot_o = orc.qr_algorithm(od, oe, None)
         chase_s = time.perf_counter() - t0
         out["oracle_chase"] = {"seconds_1_core": round(chase_s, 2), "iterations": it_o, "rotations": rot_o}
-        if args.chase_mode == 3:   # another sweep sequence: compare the sorted spectra
-            out["oracle_chase"]["eig_max_abs_diff_sorted"] = float(np.max(np.abs(np.sort(od) - np.sort(lam))))
-        else:
-            out["oracle_chase"]["eigenvalues_bit_equal"] = bool(np.array_equal(od, lam))
-        # the reference's solve on this host: its chase (the oracle, one core) plus its
-        # rotations applied at the rate of the C port of its wave kernel on all host cores,
-        # measured here on a bounded sample of an n x n apply with k = 64
-        threads = os.cpu_count() or 1
-        gf, _, _, shape = cpu_wave_gflops(n, n, 64, "f64" if args.q == "f64" else "f32", threads, target_s=4.0)
-        apply_s = 6.0 * n * rot_o / (gf * 1e9)
-        out["cpu_baseline"] = {
-            "value": round(chase_s + apply_s, 2), "unit": "s", "cores": threads, "kind": "port",
-            "sample": (f"oracle chase on 1 core ({chase_s:.2f} s, {rot_o} rotations) + those rotations "
-                       f"applied at {gf:.1f} GFLOP/s, the C port of the reference wave kernel on "
-                       f"{threads} threads over a {shape[0]} x {shape[1]} row sample, k = {shape[2]}")}
+        if n % 2 == 0 and not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_reference_solve(n, args.case, os.cpu_count() or 1, apply_every=1)
     print(json.dumps(out), flush=True)
-    h.close()
 
 
-def _tq_errors(torch, d, e, lam, Q):
-    """||TQ - Q diag(lam)||_F / ||T||_F and ||Q^T Q - I||_F in FP64 on the GPU."""
-    TQ = d[:, None] * Q
-    TQ[:-1] += e[:, None] * Q[1:]
-    TQ[1:] += e[:, None] * Q[:-1]
-    normT = math.sqrt(float((d * d).sum() + 2 * (e * e).sum()))
-    resid = float(torch.linalg.norm(TQ - Q * lam[None, :])) / normT
-    G = Q.T @ Q
-    G.diagonal().sub_(1.0)
-    return resid, float(torch.linalg.norm(G))
-
-
-def run_batched(args):
-    """Batched eigensolves (qr_algorithm_batched_, symeig_qr_batched_f64_dev): `count`
-    tridiagonals with n ~ U{32..1024}, d ~ N(0,1), e ~ U[0.1,1) (seed 3), FP64 Q, solved by
-    the persistent work-queue path with CUDA-graph rounds and the autotuned tile shapes, versus
-    one qr_algorithm! call per matrix on the same GPU, timed on a sample of the matrices and
-    extrapolated by sum n^2 (the loop over all 4096 would take about an hour).  Errors: every
-    matrix's eigenvalues against LAPACK, residual and orthogonality of a sample."""
+def measure_batched(pkg, count=4096, loop_sample=8, check=256, cpu_sample=64, with_cpu=True):
+    """Batched eigensolves (qr_algorithm_batched_, one call): `count` tridiagonals with
+    n ~ U{32..1024}, d ~ N(0,1), e ~ U[0.1,1) (seed 3), FP64 Q, against (a) one
+    qr_algorithm! call per matrix on the same GPU, timed on a sample of the batch's own
+    matrices in the reference's sweep sequence (chase mode 0) and with the multishift chase
+    (mode 3), extrapolated by sum n^2 (the apply's work per sweep is n^2 per matrix; the loop
+    over all 4096 would take about half an hour); (b) the host: the oracle's solves (timing
+    build) of a sample on all cores, extrapolated by sum n^3.  Errors: eigenvalues of `check`
+    matrices against LAPACK, residual and orthogonality of a few."""
     import torch
-    import __graft_entry__ as ge
+    from concurrent.futures import ThreadPoolExecutor
     from scipy.linalg import eigh_tridiagonal
-    pkg = ge.load_package()
-    torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     h = pkg.Handle(0)
     tuning = pkg.batched_autotune(handle=h)
     rng = np.random.default_rng(3)
-    count = args.count
     sizes = rng.integers(32, 1025, size=count)
     d = rng.standard_normal(int(sizes.sum()))
     e = rng.random(int((sizes - 1).sum())) * 0.9 + 0.1
+    doff = np.concatenate([[0], np.cumsum(sizes)])
+    eoff = np.concatenate([[0], np.cumsum(sizes - 1)])
+    qoff = np.concatenate([[0], np.cumsum(sizes * sizes)])
     td, te = torch.from_numpy(d.copy()).to(dev), torch.from_numpy(e.copy()).to(dev)
-    tQ = torch.zeros(int((sizes * sizes).sum()), dtype=torch.float64, device=dev)
-    off = 0
-    for n in sizes:
-        tQ[off:off + n * n].view(n, n).fill_diagonal_(1.0)
-        off += n * n
+    tQ = torch.zeros(int(qoff[-1]), dtype=torch.float64, device=dev)
+    for j, n in enumerate(sizes):
+        tQ[qoff[j]:qoff[j + 1]].view(n, n).fill_diagonal_(1.0)
     torch.cuda.synchronize()
-    with ClockSampler(0) as clk:
-        t0 = time.perf_counter()
-        conv, iters = pkg.qr_algorithm_batched_(td, te, sizes, tQ, handle=h)
-        torch.cuda.synchronize()
-        secs = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    conv, iters = pkg.qr_algorithm_batched_(td, te, sizes, tQ, handle=h)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
     st = h.stats()
     lam_all = td.cpu().numpy()
-    # errors: every matrix's eigenvalues vs LAPACK; residual / orthogonality on a sample
-    eig_ratio, resid_max, orth_max = 0.0, 0.0, 0.0
     eps = float(np.finfo(np.float64).eps)
-    od = oe = oq = 0
-    check = set(rng.choice(count, min(64, count), replace=False).tolist())
-    for k, n in enumerate(sizes):
-        n = int(n)
-        dk, ek = d[od:od + n], e[oe:oe + n - 1]
-        ref = eigh_tridiagonal(dk, ek, eigvals_only=True)
-        err = float(np.max(np.abs(np.sort(lam_all[od:od + n]) - ref)))
+    eig_ratio = resid_max = orth_max = 0.0
+    chk = rng.choice(count, min(check, count), replace=False)
+    for j in chk:
+        n = int(sizes[j])
+        dj, ej = d[doff[j]:doff[j + 1]], e[eoff[j]:eoff[j + 1]]
+        ref = eigh_tridiagonal(dj, ej, eigvals_only=True)
+        err = float(np.max(np.abs(np.sort(lam_all[doff[j]:doff[j + 1]]) - ref)))
         eig_ratio = max(eig_ratio, err / (10 * n * eps * float(np.max(np.abs(ref)))))
-        if k in check:
-            Qk = tQ[oq:oq + n * n].view(n, n).T
-            r, o = _tq_errors(torch, torch.from_numpy(dk).to(dev), torch.from_numpy(ek).to(dev), td[od:od + n], Qk)
-            resid_max, orth_max = max(resid_max, r / (10 * n * eps)), max(orth_max, o / (10 * n * eps))
-        od += n; oe += n - 1; oq += n * n
-    # one launch per matrix on a sample
-    sample = rng.choice(count, min(args.loop_sample, count), replace=False)
-    loop_s, work = 0.0, 0.0
-    for k in sample:
-        n = int(sizes[k])
-        dd = torch.from_numpy(rng.standard_normal(n)).to(dev)
-        ee = torch.from_numpy(rng.random(n - 1) * 0.9 + 0.1).to(dev)
-        Q = torch.eye(n, dtype=torch.float64, device=dev).T
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        pkg.qr_algorithm_(pkg.SymTridiagonal(dd, ee), Q, handle=h)
-        torch.cuda.synchronize()
-        loop_s += time.perf_counter() - t0
-        work += n * n
-    loop_est = loop_s * float((sizes.astype(np.float64) ** 2).sum()) / work
-    out = {
-        "metric": f"batched eigensolves per second, {count} tridiagonals n~U{{32..1024}}",
-        "value": round(count / secs, 2), "unit": "solves/s", "higher_is_better": True, "n_gpus": 1,
-        "dtype": "f64", "data": "synthetic (seed 3: n ~ U{32..1024}, d ~ N(0,1), e ~ U[0.1,1))",
-        "config": {"workload": "qr_algorithm_batched_ (persistent work queue, CUDA-graph rounds)",
-                   "count": count, "max_layers": 128},
-        "seconds": round(secs, 3), "all_converged": bool(conv.all()), "iterations": int(iters.sum()),
-        "rounds": st["flushes"], "tuning": tuning[0],
-        "loop": {"solves_per_s": round(count / loop_est, 3), "sample": int(len(sample)),
-                 "sample_seconds": round(loop_s, 2), "extrapolated_seconds": round(loop_est, 1)},
-        "speedup_vs_loop": round(loop_est / secs, 1),
-        "errors": {"eig_err_over_10n_eps_normT_max": eig_ratio, "resid_over_10n_eps_max": resid_max,
-                   "orth_over_10n_eps_max": orth_max, "sampled_matrices": len(check)},
-        "clocks": clk.summary(),
-    }
-    print(json.dumps(out), flush=True)
+    for j in chk[:16]:
+        n = int(sizes[j])
+        Qj = tQ[qoff[j]:qoff[j + 1]].view(n, n).T
+        r, o = _tq_errors(torch, torch.from_numpy(d[doff[j]:doff[j + 1]]).to(dev),
+                          torch.from_numpy(e[eoff[j]:eoff[j + 1]]).to(dev), td[doff[j]:doff[j + 1]], Qj)
+        resid_max, orth_max = max(resid_max, r / (10 * n * eps)), max(orth_max, o / (10 * n * eps))
+    del tQ
+    # (a) one call per matrix, on the batch's own matrices
+    sample = rng.choice(count, min(loop_sample, count), replace=False)
+    w_all = float((sizes.astype(np.float64) ** 2).sum())
+    loop = {}
+    for mode in (0, 3):
+        loop_s, work = 0.0, 0.0
+        for j in sample:
+            n = int(sizes[j])
+            dd = torch.from_numpy(d[doff[j]:doff[j + 1]].copy()).to(dev)
+            ee = torch.from_numpy(e[eoff[j]:eoff[j + 1]].copy()).to(dev)
+            Q = torch.eye(n, dtype=torch.float64, device=dev).T
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            pkg.qr_algorithm_(pkg.SymTridiagonal(dd, ee), Q, handle=h, chase_mode=mode)
+            torch.cuda.synchronize()
+            loop_s += time.perf_counter() - t0
+            work += n * n
+        est = loop_s * w_all / work
+        loop[f"mode{mode}"] = {"solves_per_s": round(count / est, 3), "sample": int(len(sample)),
+                               "sample_seconds": round(loop_s, 2), "extrapolated_seconds": round(est, 1)}
     h.close()
+    best_loop = min(loop["mode0"]["extrapolated_seconds"], loop["mode3"]["extrapolated_seconds"])
+    out = {"value": round(count / secs, 2), "unit": "solves/s", "count": count, "seconds": round(secs, 3),
+           "all_converged": bool(conv.all()), "iterations": int(iters.sum()), "rounds": st["flushes"],
+           "tuning": tuning[0], "loop": loop,
+           "speedup_vs_loop_mode0": round(loop["mode0"]["extrapolated_seconds"] / secs, 1),
+           "speedup_vs_best_loop": round(best_loop / secs, 1),
+           "errors": {"eig_err_over_10n_eps_normT_max": eig_ratio, "eig_checked": int(len(chk)),
+                      "resid_over_10n_eps_max": resid_max, "orth_over_10n_eps_max": orth_max,
+                      "vectors_checked": 16}}
+    if with_cpu:
+        from oracle import oracle as orc
+        threads = os.cpu_count() or 1
+        cs = rng.choice(count, min(cpu_sample, count), replace=False)
+
+        def one(j):
+            n = int(sizes[j])
+            Qj = np.asfortranarray(np.eye(n))
+            orc.qr_algorithm(d[doff[j]:doff[j + 1]].copy(), e[eoff[j]:eoff[j + 1]].copy(), Qj, fast=True)
+
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(one, cs))
+        cpu_s = time.perf_counter() - t0
+        w3 = float((sizes.astype(np.float64) ** 3).sum())
+        est = cpu_s * w3 / float((sizes[cs].astype(np.float64) ** 3).sum())
+        out["cpu_baseline"] = {"value": round(count / est, 3), "unit": "solves/s", "cores": threads, "kind": "port",
+                               "sample": (f"{len(cs)} of the matrices solved by the oracle (timing build, "
+                                          f"chase + layer-major apply per flush) on {threads} threads, "
+                                          f"{cpu_s:.1f} s, extrapolated by sum n^3")}
+        out["speedup_vs_cpu"] = round(est / secs, 1)
+    return out
 
 
-def run_adjoint(args):
+def run_batched(args):
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    torch.cuda.set_device(0)
+    with ClockSampler(0) as clk:
+        r = measure_batched(pkg, args.count, args.loop_sample, with_cpu=not args.no_cpu_baseline)
+    out = {"metric": f"batched eigensolves per second, {args.count} tridiagonals n~U{{32..1024}}",
+           "higher_is_better": True, "n_gpus": 1, "dtype": "f64",
+           "data": "synthetic (seed 3: n ~ U{32..1024}, d ~ N(0,1), e ~ U[0.1,1))",
+           "config": {"workload": "qr_algorithm_batched_ (persistent work queue, CUDA-graph rounds)",
+                      "count": args.count, "max_layers": 128}, **r, "clocks": clk.summary()}
+    print(json.dumps(out), flush=True)
+
+
+def measure_adjoint(pkg, n=4096, K=64, chase_mode=3, batched=True, with_cpu=True):
     """Adjoint of the eigensolve (TridiagEigh: forward qr_algorithm!, backward
     symeig_eig_adjoint_f64_dev): n = 4096, d ~ N(0,1), e ~ U[0.1,1) (seed 4), loss
     L = sum_i w_i lam_(i) + sum_{i<=64} q_(i)^T B q_(i), w ~ N(0,1), B symmetric ~ N(0,1/n),
-    eigenpairs sorted ascending.  Reports (forward + backward) / forward time and the gradient
-    against an FP64 reference (LAPACK eigenpairs and the closed-form pullback in numpy); the
-    finite-difference check runs in the tests at smaller n.  Then the batched variant
-    (TridiagEighBatched) on 256 matrices of n = 512."""
+    eigenpairs sorted ascending.  (forward + backward) / forward time, the gradient against an
+    FP64 reference (LAPACK eigenpairs and the closed-form pullback in numpy), the adjoint GEMMs
+    against the measured FP64 MMA peak; optionally the batched variant (256 x n = 512) and the
+    host's forward + backward (the reference's solve path, then the pullback by numpy BLAS)."""
     import torch
-    import __graft_entry__ as ge
     from scipy.linalg import eigh_tridiagonal
-    pkg = ge.load_package()
-    torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
-    n, K = (args.n if args.n != 16384 else 4096), 64
     rng = np.random.default_rng(4)
     d = rng.standard_normal(n)
     e = rng.random(n - 1) * 0.9 + 0.1
@@ -701,27 +833,27 @@ def run_adjoint(args):
     # one untimed pass of the whole path at n = 256 (library and kernel loading)
     wd = torch.tensor(d[:256], device=dev, requires_grad=True)
     we = torch.tensor(e[:255], device=dev, requires_grad=True)
-    wl, wQ = pkg.TridiagEigh.apply(wd, we)
+    wl, wQ = pkg.TridiagEigh.apply(wd, we, chase_mode)
     wo = torch.argsort(wl)
     wK = wQ[:, wo][:, :K]
     ((tw[:256] * wl[wo]).sum() + (wK * (tB[:256, :256] @ wK)).sum()).backward()
     torch.cuda.synchronize()
     td = torch.tensor(d, device=dev, requires_grad=True)
     te = torch.tensor(e, device=dev, requires_grad=True)
-    with ClockSampler(0) as clk:
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        lam, Q = pkg.TridiagEigh.apply(td, te)
-        torch.cuda.synchronize()
-        t1 = time.perf_counter()
-        L = loss(lam, Q)
-        torch.cuda.synchronize()
-        tl = time.perf_counter()
-        L.backward()
-        torch.cuda.synchronize()
-        t2 = time.perf_counter()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lam, Q = pkg.TridiagEigh.apply(td, te, chase_mode)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    L = loss(lam, Q)
+    torch.cuda.synchronize()
+    tl = time.perf_counter()
+    L.backward()
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
     fwd, loss_s, bwd = t1 - t0, tl - t1, t2 - tl
     # FP64 reference gradient
+    tr0 = time.perf_counter()
     lam_r, V = eigh_tridiagonal(d, e)
     gV = np.zeros((n, n))
     gV[:, :K] = 2 * Bm @ V[:, :K]
@@ -731,6 +863,7 @@ def run_adjoint(args):
     np.fill_diagonal(F, 0.0)
     A = V @ (np.diag(w) + F * (V.T @ gV)) @ V.T
     g_ref = np.concatenate([np.diag(A), np.diag(A, 1) + np.diag(A, -1)])
+    ref_s = time.perf_counter() - tr0
     g = np.concatenate([td.grad.cpu().numpy(), te.grad.cpu().numpy()])
     rel = float(np.linalg.norm(g - g_ref) / np.linalg.norm(g_ref))
     # the adjoint kernels alone (two FP64 tensor-core GEMMs with fused epilogues)
@@ -745,47 +878,83 @@ def run_adjoint(args):
     torch.cuda.synchronize()
     adj_ms = e0.elapsed_time(e1)
     dmma_peak = pkg._lib.measure_dmma_peak(0)
-    # batched variant: 256 matrices of n = 512
-    B, nb = 256, 512
-    db = torch.tensor(rng.standard_normal((B, nb)), device=dev, requires_grad=True)
-    eb = torch.tensor(rng.random((B, nb - 1)) * 0.9 + 0.1, device=dev, requires_grad=True)
-    wb = torch.tensor(rng.standard_normal((B, nb)), device=dev)
-    Bb = torch.tensor(rng.standard_normal((nb, nb)) / np.sqrt(nb), device=dev)
-    Bb = (Bb + Bb.T) / 2
-    # untimed pass of the batched path on 4 matrices
-    w4d, w4e = db[:4].detach().clone().requires_grad_(True), eb[:4].detach().clone().requires_grad_(True)
-    l4, Q4 = pkg.TridiagEighBatched.apply(w4d, w4e)
-    o4 = torch.argsort(l4, dim=1)
-    K4 = torch.gather(Q4, 2, o4[:, None, :8].expand(4, nb, 8))
-    ((wb[:4] * torch.gather(l4, 1, o4)).sum() + (K4 * (Bb @ K4)).sum()).backward()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    lamb, Qb = pkg.TridiagEighBatched.apply(db, eb)
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    ob = torch.argsort(lamb, dim=1)
-    QKb = torch.gather(Qb, 2, ob[:, None, :8].expand(B, nb, 8))
-    Lb = (wb * torch.gather(lamb, 1, ob)).sum() + (QKb * (Bb @ QKb)).sum()
-    Lb.backward()
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    out = {
-        "metric": f"adjoint (forward + backward) / forward time, n={n}",
-        "value": round((fwd + loss_s + bwd) / fwd, 4), "unit": "ratio", "higher_is_better": False, "n_gpus": 1,
-        "dtype": "f64", "data": "synthetic (seed 4: d ~ N(0,1), e ~ U[0.1,1), w ~ N(0,1), B ~ N(0,1/n) symmetric)",
-        "config": {"workload": "TridiagEigh forward + backward, loss on the 64 lowest eigenpairs", "n": n, "K": K},
-        "forward_s": round(fwd, 3), "loss_s": round(loss_s, 3), "backward_s": round(bwd, 3),
-        "grad_rel_err_vs_fp64_reference": rel,
-        "adjoint_kernels_ms": round(adj_ms, 2),
-        "adjoint_gemm_tflops": round(4.0 * n ** 3 / (adj_ms * 1e-3) / 1e12, 3),
-        "roofline": {"bound": "fp64 tensor (mma.sync .f64)", "achieved": round(4.0 * n ** 3 / (adj_ms * 1e-3) / 1e12, 3),
-                     "peak": round(dmma_peak, 3), "unit": "TFLOP/s",
-                     "frac": round(4.0 * n ** 3 / (adj_ms * 1e-3) / 1e12 / dmma_peak, 4),
-                     "peak_source": "measured now by symeig_measure_dmma_peak"},
-        "batched": {"B": B, "n": nb, "forward_s": round(t1 - t0, 3), "backward_s": round(t2 - t1, 3),
-                    "ratio": round((t2 - t0) / (t1 - t0), 4)},
-        "clocks": clk.summary(),
-    }
+    del gQ, Q, Q_d
+    out = {"value": round((fwd + loss_s + bwd) / fwd, 4), "unit": "ratio", "n": n, "K": K,
+           "forward_chase_mode": chase_mode,
+           "forward_s": round(fwd, 3), "loss_s": round(loss_s, 3), "backward_s": round(bwd, 3),
+           "grad_rel_err_vs_fp64_reference": rel, "fp64_reference_host_s": round(ref_s, 2),
+           "adjoint_kernels_ms": round(adj_ms, 2),
+           "roofline": {"bound": "fp64 tensor (mma.sync .f64)", "achieved": round(4.0 * n ** 3 / (adj_ms * 1e-3) / 1e12, 3),
+                        "peak": round(dmma_peak, 3), "unit": "TFLOP/s",
+                        "frac": round(4.0 * n ** 3 / (adj_ms * 1e-3) / 1e12 / dmma_peak, 4),
+                        "peak_source": "measured now by symeig_measure_dmma_peak"}}
+    if batched:
+        B, nb = 256, 512
+        db = torch.tensor(rng.standard_normal((B, nb)), device=dev, requires_grad=True)
+        eb = torch.tensor(rng.random((B, nb - 1)) * 0.9 + 0.1, device=dev, requires_grad=True)
+        wb = torch.tensor(rng.standard_normal((B, nb)), device=dev)
+        Bb = torch.tensor(rng.standard_normal((nb, nb)) / np.sqrt(nb), device=dev)
+        Bb = (Bb + Bb.T) / 2
+        w4d, w4e = db[:4].detach().clone().requires_grad_(True), eb[:4].detach().clone().requires_grad_(True)
+        l4, Q4 = pkg.TridiagEighBatched.apply(w4d, w4e)
+        o4 = torch.argsort(l4, dim=1)
+        K4 = torch.gather(Q4, 2, o4[:, None, :8].expand(4, nb, 8))
+        ((wb[:4] * torch.gather(l4, 1, o4)).sum() + (K4 * (Bb @ K4)).sum()).backward()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lamb, Qb = pkg.TridiagEighBatched.apply(db, eb)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        ob = torch.argsort(lamb, dim=1)
+        QKb = torch.gather(Qb, 2, ob[:, None, :8].expand(B, nb, 8))
+        Lb = (wb * torch.gather(lamb, 1, ob)).sum() + (QKb * (Bb @ QKb)).sum()
+        Lb.backward()
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        out["batched"] = {"B": B, "n": nb, "forward_s": round(t1 - t0, 3), "backward_s": round(t2 - t1, 3),
+                          "ratio": round((t2 - t0) / (t1 - t0), 4)}
+    if with_cpu and n % 2 == 0:
+        # the host's forward (the reference's solve path) and backward (numpy BLAS pullback)
+        from oracle import oracle as orc
+        threads = os.cpu_count() or 1
+        dd, ee = d.copy(), e.copy()
+        Qh = np.asfortranarray(np.eye(n))
+        t0 = time.perf_counter()
+        orc.qr_reference_path(dd, ee, Qh, nthreads=threads, fast=True)  # every flush applied
+        t1 = time.perf_counter()
+        order = np.argsort(dd)
+        Vh = Qh[:, order]
+        gVh = np.zeros((n, n))
+        gVh[:, :K] = 2 * Bm @ Vh[:, :K]
+        lh = dd[order]
+        Fh = lh[None, :] - lh[:, None]
+        np.fill_diagonal(Fh, 1.0)
+        Fh = 1.0 / Fh
+        np.fill_diagonal(Fh, 0.0)
+        Ah = Vh @ (np.diag(w) + Fh * (Vh.T @ gVh)) @ Vh.T
+        t2 = time.perf_counter()
+        out["cpu_baseline"] = {"value": round(t2 - t0, 3), "unit": "s (forward + backward)", "cores": threads,
+                               "kind": "port", "forward_s": round(t1 - t0, 3), "backward_s": round(t2 - t1, 3),
+                               "sample": ("the whole workload: the reference's solve path (oracle timing build, "
+                                          f"{threads} threads) and the closed-form pullback in numpy BLAS")}
+        out["speedup_vs_cpu"] = round((t2 - t0) / (fwd + loss_s + bwd), 1)
+    return out
+
+
+def run_adjoint(args):
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.load_package()
+    torch.cuda.set_device(0)
+    n = args.n if args.n != 16384 else 4096
+    with ClockSampler(0) as clk:
+        r = measure_adjoint(pkg, n, 64, 3 if args.chase_mode is None else args.chase_mode,
+                            with_cpu=not args.no_cpu_baseline)
+    out = {"metric": f"adjoint (forward + backward) / forward time, n={n}", "higher_is_better": False,
+           "n_gpus": 1, "dtype": "f64",
+           "data": "synthetic (seed 4: d ~ N(0,1), e ~ U[0.1,1), w ~ N(0,1), B ~ N(0,1/n) symmetric)",
+           "config": {"workload": "TridiagEigh forward + backward, loss on the 64 lowest eigenpairs", "n": n, "K": 64},
+           **r, "clocks": clk.summary()}
     print(json.dumps(out), flush=True)
 
 
@@ -799,6 +968,8 @@ def run_dense(args):
     import __graft_entry__ as ge
     from scipy.linalg import lapack
     pkg = ge.load_package()
+    if args.chase_mode is None:
+        args.chase_mode = 0
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     n = args.n if args.n != 16384 else 4096

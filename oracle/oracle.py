@@ -15,8 +15,12 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 LIB_PATH = HERE / "_build" / "liboracle.so"
+# the same source built for timing only (contraction allowed, tuned for the host's cores):
+# the CPU baselines run it; the checks never do
+FAST_LIB_PATH = HERE / "_build" / "liboracle_fast.so"
 
 _lib = None
+_fast = None
 
 c_i64 = ctypes.c_int64
 c_i32 = ctypes.c_int32
@@ -27,16 +31,30 @@ c_vp = ctypes.c_void_p
 def build(force: bool = False) -> Path:
     """Compile the oracle with its Makefile (gcc; a second or two)."""
     src = HERE / "symeig_oracle.c"
-    if force or not LIB_PATH.exists() or LIB_PATH.stat().st_mtime < src.stat().st_mtime:
+    deps = [src, HERE / "Makefile"]
+    stale = any(not p.exists() or any(p.stat().st_mtime < d.stat().st_mtime for d in deps)
+                for p in (LIB_PATH, FAST_LIB_PATH))
+    if force or stale:
         subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
     return LIB_PATH
 
 
-def lib():
-    global _lib
+def lib(fast: bool = False):
+    """The checker library, or with fast=True the timing build of the same source."""
+    global _lib, _fast
+    if fast:
+        if _fast is None:
+            build()
+            _fast = _bind(ctypes.CDLL(str(FAST_LIB_PATH)))
+        return _fast
     if _lib is None:
         build()
-        L = ctypes.CDLL(str(LIB_PATH))
+        _lib = _bind(ctypes.CDLL(str(LIB_PATH)))
+    return _lib
+
+
+def _bind(L):
+    if True:
         L.oracle_givens.argtypes = [c_dbl, c_dbl, ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl), ctypes.POINTER(c_dbl)]
         L.oracle_givens.restype = None
         for name in ("oracle_apply_seq_f64", "oracle_apply_seq_f32"):
@@ -70,8 +88,13 @@ def lib():
         L.oracle_qr_timeorder.argtypes = [c_vp, c_vp, c_i64, c_vp, c_i64, c_i64, c_i32, c_dbl, c_i64,
                                           ctypes.POINTER(c_i32), ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)]
         L.oracle_qr_timeorder.restype = ctypes.c_int
-        _lib = L
-    return _lib
+        L.oracle_qr_reference_path.argtypes = [c_vp, c_vp, c_i64, c_vp, c_i64, c_i64, c_i32, c_dbl, c_i64,
+                                               ctypes.c_int, c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(c_i64),
+                                               ctypes.POINTER(c_i64), ctypes.POINTER(c_dbl),
+                                               ctypes.POINTER(c_dbl), ctypes.POINTER(c_i64),
+                                               ctypes.POINTER(c_i64)]
+        L.oracle_qr_reference_path.restype = ctypes.c_int
+    return L
 
 
 def _ptr(a: np.ndarray) -> int:
@@ -126,15 +149,17 @@ def apply_scaled(Q: np.ndarray, cs: np.ndarray) -> None:
         raise RuntimeError(f"oracle_apply_scaled_f64 failed with status {rc}")
 
 
-def apply_wave(Q: np.ndarray, cs: np.ndarray, nthreads: int = 1) -> None:
+def apply_wave(Q: np.ndarray, cs: np.ndarray, nthreads: int = 1, fast: bool = False) -> None:
     """The wave-order fused apply itself (src/wave.jl:36-162, src/bulk_givens.jl), with the
-    reference's row-slab threading.  Requires odd n-1 and even k, as the reference asserts."""
+    reference's row-slab threading.  Requires odd n-1 and even k, as the reference asserts.
+    fast=True runs the timing build (contracted arithmetic: for CPU baselines only)."""
     _check_q(Q)
     m, n = Q.shape
     k = cs.shape[1]
     flat = np.ascontiguousarray(np.transpose(cs, (1, 0, 2)).reshape(-1), dtype=Q.dtype)
     ld = Q.strides[1] // Q.itemsize if n > 1 else max(m, 1)
-    fn = lib().oracle_apply_wave_f64 if Q.dtype == np.float64 else lib().oracle_apply_wave_f32
+    L = lib(fast)
+    fn = L.oracle_apply_wave_f64 if Q.dtype == np.float64 else L.oracle_apply_wave_f32
     rc = fn(_ptr(Q), ld, m, n, _ptr(flat), k, nthreads)
     if rc != 0:
         raise AssertionError("wave order needs n-1 odd and k even (src/wave.jl:65-66)")
@@ -190,12 +215,13 @@ def qr_timeorder(d: np.ndarray, e: np.ndarray, Q: np.ndarray, max_layers: int = 
 
 def qr_algorithm(d: np.ndarray, e: np.ndarray, Q: np.ndarray | None, max_layers: int = 128,
                  tol: float | None = None, maxiter: int | None = None, exact_order: bool = True,
-                 apply_form: int = 0):
+                 apply_form: int = 0, fast: bool = False):
     """qr_algorithm!(SymTridiagonal(d, e), Q, max_layers, tol, maxiter)
     (src/bulge_chasing.jl:146-288): d, e and Q updated in place.  exact_order=False keeps the
     reference's grid placement (rotation i of a sweep at layer ++thickness[i]); True (default)
     places each sweep at one layer so the grid's layer-major order is the chase's order.
-    apply_form=1 applies each flush in the device's scaled form (FP64 Q only).
+    apply_form=1 applies each flush in the device's scaled form (FP64 Q only).  fast=True runs
+    the timing build (CPU baselines only: its contracted arithmetic is not the reference's).
     Returns (converged, iter, flushes, rotations)."""
     n = d.shape[0]
     assert d.dtype == np.float64 and e.dtype == np.float64 and e.shape[0] == max(n - 1, 0)
@@ -210,7 +236,7 @@ def qr_algorithm(d: np.ndarray, e: np.ndarray, Q: np.ndarray | None, max_layers:
     else:
         m, ld, qp, is32 = 0, 1, None, 0
     ebuf = e if e.size else np.zeros(1)
-    rc = lib().oracle_qr_form(_ptr(d), _ptr(ebuf), n, qp, ld, m, is32, max_layers, tol, maxiter, int(exact_order),
+    rc = lib(fast).oracle_qr_form(_ptr(d), _ptr(ebuf), n, qp, ld, m, is32, max_layers, tol, maxiter, int(exact_order),
                               int(apply_form), ctypes.byref(conv), ctypes.byref(it), ctypes.byref(fl),
                               ctypes.byref(rot))
     if rc != 0:
@@ -244,3 +270,33 @@ def qr_multishift(d: np.ndarray, e: np.ndarray, Q: np.ndarray | None, max_layers
     if rc != 0:
         raise RuntimeError(f"oracle_qr_multishift failed with status {rc}")
     return bool(conv.value), it.value, fl.value, rot.value, bat.value
+
+
+def qr_reference_path(d: np.ndarray, e: np.ndarray, Q: np.ndarray | None, max_layers: int = 128,
+                      nthreads: int = 1, fast: bool = True, apply_every: int = 1):
+    """The reference's solve path on the host, timed (oracle_qr_reference_path): its chase and
+    grid placement, and every flush's whole (n-1) x max_layers grid applied by the row-slab
+    threaded wave kernel (src/bulge_chasing.jl:146-288 -> src/wave.jl:36-60).  Even n only,
+    as the reference.  d, e, Q updated in place.  fast=True (default) uses the timing build.
+    apply_every > 1 applies only every apply_every-th flush (a timing sample; Q is then not
+    the solve's Q).  Returns (converged, iter, flushes, chase_seconds, apply_seconds,
+    rotations_of_applied_flushes, rotations_of_all_flushes)."""
+    n = d.shape[0]
+    assert d.dtype == np.float64 and e.dtype == np.float64 and e.shape[0] == n - 1
+    conv, it, fl = c_i32(), c_i64(), c_i64()
+    tc, ta = c_dbl(), c_dbl()
+    ra, rt = c_i64(), c_i64()
+    if Q is not None:
+        _check_q(Q)
+        assert Q.dtype == np.float64
+        m, ld, qp = Q.shape[0], Q.strides[1] // Q.itemsize, _ptr(Q)
+    else:
+        m, ld, qp = 0, 1, None
+    rc = lib(fast).oracle_qr_reference_path(_ptr(d), _ptr(e), n, qp, ld, m, int(max_layers),
+                                            float(np.finfo(np.float64).eps), 100 * n, int(nthreads),
+                                            int(apply_every), ctypes.byref(conv), ctypes.byref(it),
+                                            ctypes.byref(fl), ctypes.byref(tc), ctypes.byref(ta),
+                                            ctypes.byref(ra), ctypes.byref(rt))
+    if rc != 0:
+        raise ValueError(f"oracle_qr_reference_path: status {rc} (even n and even max_layers needed)")
+    return bool(conv.value), it.value, fl.value, tc.value, ta.value, ra.value, rt.value

@@ -53,12 +53,14 @@
  *                       placement rules.  Checked by the reference's error bounds, and by the
  *                       reference's bits where no block takes a batch.
  */
+#define _POSIX_C_SOURCE 200809L
 #include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 #include <pthread.h>
+#include <time.h>
 
 /* ------------------------------------------------------------------------------------ */
 /* givensAlgorithm (LinearAlgebra, DLARTG 3.2 port); call site src/simple_givens.jl:21   */
@@ -738,6 +740,65 @@ static int oracle_qr_driver(double* d, double* e, int64_t n, void* Q, int64_t ld
     if (rotations) *rotations = st.total_rotations;
     if (batches) *batches = st.batches;
     free(givens); free(g32); free(thick); free(place);
+    return 0;
+}
+
+/* The reference's own solve path, for timing on the host (the CPU baseline of the full
+ * eigensolve): qr_algorithm! exactly as src/bulge_chasing.jl:146-288 runs it -- the
+ * reference's grid placement (givens[i, ++layer_thickness[i]]), a grid of (n-1) x max_layers
+ * filled with (1, 0) at every flush (:169), and each flush applied as a whole by the
+ * row-slab threaded wave kernel, bulk_wave_order_2x2_rmul_parallel!(Q, givens) (:282,
+ * src/wave.jl:36-60), on nthreads threads.  Needs even n and even max_layers, as the
+ * reference asserts (:155, src/wave.jl:65-66); returns 1 otherwise.  The chase and the applies
+ * are timed separately (seconds of wall clock).  apply_every > 1 applies only every
+ * apply_every-th flush (a timing sample: the chase never reads Q, and the wave kernel's cost
+ * depends on the grid only, about in proportion to its rotations); *rot_applied and
+ * *rot_total count the rotations of the applied flushes and of all flushes. */
+static double now_seconds(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+int oracle_qr_reference_path(double* d, double* e, int64_t n, double* Q, int64_t ldq, int64_t m,
+                             int32_t max_layers, double tol, int64_t maxiter, int nthreads,
+                             int32_t apply_every, int32_t* converged, int64_t* iter, int64_t* flushes,
+                             double* chase_seconds, double* apply_seconds, int64_t* rot_applied,
+                             int64_t* rot_total)
+{
+    if (n < 2 || n % 2 != 0 || max_layers < 2 || max_layers % 2 != 0 || (Q && ldq < m)) return 1;
+    oracle_qr_state st;
+    oracle_qr_init(&st, n, max_layers, tol, maxiter, 0);
+    const int64_t nr = n - 1;
+    double* givens = (double*)malloc(sizeof(double) * 2 * nr * max_layers);
+    int64_t* thick = (int64_t*)malloc(sizeof(int64_t) * n);
+    int64_t* place = (int64_t*)malloc(sizeof(int64_t) * n);
+    if (!givens || !thick || !place) { free(givens); free(thick); free(place); return -2; }
+    double tc = 0.0, ta = 0.0;
+    int64_t ra = 0, f = 0;
+    if (apply_every < 1) apply_every = 1;
+    *converged = 1;
+    for (;; ++f) {
+        double t0 = now_seconds();
+        int rc = oracle_qr_flush(&st, d, e, givens, thick, place);
+        tc += now_seconds() - t0;
+        if (rc < 0) { *converged = 0; break; }
+        if (rc == 0) break;
+        if (Q && m > 0 && f % apply_every == 0) {
+            t0 = now_seconds();
+            wave_parallel(Q, ldq, m, n, givens, max_layers, nthreads, 0);
+            ta += now_seconds() - t0;
+            ra += st.rotations;
+        }
+    }
+    if (rot_applied) *rot_applied = ra;
+    if (rot_total) *rot_total = st.total_rotations;
+    *iter = st.iter;
+    if (flushes) *flushes = st.flush_count;
+    if (chase_seconds) *chase_seconds = tc;
+    if (apply_seconds) *apply_seconds = ta;
+    free(givens); free(thick); free(place);
     return 0;
 }
 
