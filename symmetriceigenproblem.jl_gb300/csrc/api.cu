@@ -62,7 +62,10 @@ struct symeig_context {
     cudaStream_t pipe[kPipeBlocks] = {};
     cudaEvent_t pipe_done[kPipeBlocks] = {};
     cudaEvent_t ev_table = nullptr;
-    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs, bak, rot, dense, dense_io, bulge;
+    // the column-segment pipeline of the host-pointer apply: per segment, columns copied in and
+    // kernel done
+    cudaEvent_t seg_in[kPipeBlocks] = {}, seg_done[kPipeBlocks] = {};
+    DevBuf grid[2], thick[2], place[2], table, state, d, e, q, cs, bak, rot, dense, dense_io, bulge, seg_state;
     int* derr = nullptr;   // device error word of the wave kernels (bounded waits)
     int32_t exact_order = 1;  // rotation placement of the qr driver
     int32_t chase_mode = 0;   // symeig_set_chase_mode
@@ -423,63 +426,41 @@ int apply_dev(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T*
     return apply_grid<T, T>(h, A, lda, m, cs, n - 1, nullptr, 0, n, k, h->stream);
 }
 
-// One pass (k <= 64 layers) with host Q, pipelined over kPipeBlocks row blocks: column
-// rotations act on every row alike, so rows [r0, r1) of Q are an independent problem.  Each
-// block has its own stream: its host-to-device copy starts at once, its wave kernel waits for
-// the one table (built on the main stream from the (c,s) grid), and its device-to-host copy
-// follows its kernel.  Copies in both directions then overlap the kernels of other blocks, so
-// the call costs about one kernel plus one block's copies instead of both copies plus the
-// kernel.  A single block keeps the FP64 units busy (1024 rows of 16384 are 64 CTAs of 4 warps,
-// and the blocks' kernels overlap one another).
+// One pass (k <= 64 layers) with host Q, pipelined by column segments (apply_host_segmented,
+// apply.cu): the columns of Q go to the device in kPipeBlocks chunks on one copy stream, the
+// pass runs as kPipeBlocks launches of the whole-matrix wave kernel (each waiting only for the
+// columns it reads, carrying its registers to the next in a state buffer), and the columns
+// each launch finishes go back on a second copy stream right after it.  The copies in both
+// directions then overlap the kernels, which run at the full-matrix rate.
 template <typename T>
 int apply_host_pipelined(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T* cs, int64_t k)
 {
     cudaStream_t s = h->stream;
     begin_call(h);
-    for (int b = 0; b < kPipeBlocks; ++b) {
+    for (int b = 0; b < 2; ++b)
         if (!h->pipe[b]) CK(cudaStreamCreateWithFlags(&h->pipe[b], cudaStreamNonBlocking));
-        if (!h->pipe_done[b]) CK(cudaEventCreateWithFlags(&h->pipe_done[b], cudaEventDisableTiming));
+    for (int j = 0; j < kPipeBlocks; ++j) {
+        if (!h->seg_in[j]) CK(cudaEventCreateWithFlags(&h->seg_in[j], cudaEventDisableTiming));
+        if (!h->seg_done[j]) CK(cudaEventCreateWithFlags(&h->seg_done[j], cudaEventDisableTiming));
     }
-    if (!h->ev_table) CK(cudaEventCreateWithFlags(&h->ev_table, cudaEventDisableTiming));
-    T* q = (T*)h->q.ptr;
-    // the blocks start after whatever the caller queued on the main stream before this call
+    if (!h->pipe_done[0]) CK(cudaEventCreateWithFlags(&h->pipe_done[0], cudaEventDisableTiming));
+    CK(h->seg_state.ensure(apply_segment_state_bytes<T>(m)));
+    CK(h->table.ensure(apply_table_bytes<T>(n, k)));
+    // the copies start after whatever the caller queued on the main stream before this call
     CK(cudaEventRecord(h->ev_main, s));
+    CK(cudaStreamWaitEvent(h->pipe[0], h->ev_main, 0));
+    CK(cudaStreamWaitEvent(h->pipe[1], h->ev_main, 0));
     const size_t cs_bytes = (size_t)(n - 1) * k * 2 * sizeof(T);
     CK(cudaMemcpyAsync(h->cs.ptr, cs, cs_bytes, cudaMemcpyHostToDevice, s));
-    CK(h->table.ensure(apply_table_bytes<T>(n, k)));
     ApplyPass pass{0, n, 0, k, 1};
     pass.form = sizeof(T) == 8 ? h->apply_form : 0;
     pass.stall = h->test_stall;
-    CK((apply_pass<T, T>(q, m, m, (const T*)h->cs.ptr, n - 1, nullptr, pass, h->table.ptr, h->derr, s,
-                         nullptr, nullptr, kPassTable)));
-    CK(cudaEventRecord(h->ev_table, s));
-    // copies in and kernels of every block first, then the copies out: a copy to pageable host
-    // memory blocks the calling thread, and must not hold back the next block's copy in
-    const int64_t rows = ((m + kPipeBlocks - 1) / kPipeBlocks + 63) / 64 * 64;
-    int used = 0;
-    for (int b = 0; b < kPipeBlocks; ++b) {
-        const int64_t r0 = (int64_t)b * rows;
-        if (r0 >= m) break;
-        const int64_t mb = std::min(rows, m - r0);
-        cudaStream_t sb = h->pipe[b];
-        CK(cudaStreamWaitEvent(sb, h->ev_main, 0));
-        CK(cudaMemcpy2DAsync(q + r0, m * sizeof(T), A + r0, lda * sizeof(T), mb * sizeof(T), n,
-                             cudaMemcpyHostToDevice, sb));
-        CK(cudaStreamWaitEvent(sb, h->ev_table, 0));
-        CK((apply_pass<T, T>(q + r0, m, mb, (const T*)h->cs.ptr, n - 1, nullptr, pass, h->table.ptr, h->derr,
-                             sb, nullptr, nullptr, kPassWave)));
-        ++used;
-    }
-    for (int b = 0; b < used; ++b) {
-        const int64_t r0 = (int64_t)b * rows;
-        const int64_t mb = std::min(rows, m - r0);
-        cudaStream_t sb = h->pipe[b];
-        CK(cudaMemcpy2DAsync(A + r0, lda * sizeof(T), q + r0, m * sizeof(T), mb * sizeof(T), n,
-                             cudaMemcpyDeviceToHost, sb));
-        CK(cudaEventRecord(h->pipe_done[b], sb));
-    }
-    for (int b = 0; b < used; ++b) CK(cudaStreamWaitEvent(s, h->pipe_done[b], 0));
-    h->stats.wave_launches += used;
+    HostStream io{A, lda, h->pipe[0], h->pipe[1], h->seg_in, h->seg_done, kPipeBlocks, h->seg_state.ptr};
+    CK(apply_host_segmented<T>((T*)h->q.ptr, m, (const T*)h->cs.ptr, pass, h->table.ptr, h->derr, s, io));
+    // the call ends when the last copy out has landed
+    CK(cudaEventRecord(h->pipe_done[0], h->pipe[1]));
+    CK(cudaStreamWaitEvent(s, h->pipe_done[0], 0));
+    h->stats.wave_launches += kPipeBlocks;
     h->stats.applied_rotation_rows += (n - 1) * k * m;
     return SYMEIG_OK;
 }
@@ -505,7 +486,7 @@ int apply_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T
         rc = apply_host_pipelined<T>(h, A, lda, m, n, cs, k);
         if (rc) {
             // nothing queued may still read or write the caller's buffer after the return
-            for (int b = 0; b < kPipeBlocks; ++b)
+            for (int b = 0; b < 2; ++b)
                 if (h->pipe[b]) cudaStreamSynchronize(h->pipe[b]);
             cudaStreamSynchronize(s);
             return rc;
@@ -684,7 +665,7 @@ int symeig_destroy(symeig_handle h)
     }
     h->table.release(); h->state.release(); h->d.release(); h->e.release();
     h->q.release(); h->cs.release(); h->bak.release(); h->rot.release();
-    h->dense.release(); h->dense_io.release(); h->bulge.release();
+    h->dense.release(); h->dense_io.release(); h->bulge.release(); h->seg_state.release();
     if (h->ev_main) cudaEventDestroy(h->ev_main);
     for (int b = 0; b < kPipeBlocks; ++b) {
         if (h->pipe[b]) {
@@ -692,6 +673,8 @@ int symeig_destroy(symeig_handle h)
             cudaStreamDestroy(h->pipe[b]);
         }
         if (h->pipe_done[b]) cudaEventDestroy(h->pipe_done[b]);
+        if (h->seg_in[b]) cudaEventDestroy(h->seg_in[b]);
+        if (h->seg_done[b]) cudaEventDestroy(h->seg_done[b]);
     }
     if (h->ev_table) cudaEventDestroy(h->ev_table);
     for (cudaEvent_t ev : h->timing) cudaEventDestroy(ev);

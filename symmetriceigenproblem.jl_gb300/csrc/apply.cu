@@ -298,11 +298,15 @@ scaled_table_kernel(unsigned char* __restrict__ table, int64_t n_chunks, const T
     }
 }
 
+// One launch covers chunks [c_begin, c_end) of the pass (all of them unless the pass runs as
+// column segments, see wave_tile); `state` holds the registers carried between segments,
+// segment_state_values * THREADS values per CTA.
 template <typename T, int S, bool SCALED = false, bool INT_MUL = false>
 __global__ void __launch_bounds__(Cfg<T, S>::THREADS, INT_MUL ? Cfg<T, S>::MINB_INT : Cfg<T, S>::MINB)
 wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
                   const unsigned char* __restrict__ table, int32_t n_chunks, int* __restrict__ err,
-                  const T nz, int64_t rs, int32_t stall)
+                  const T nz, int64_t rs, int32_t stall, int32_t c_begin, int32_t c_end,
+                  T* __restrict__ state)
 {
     using Sh = typename Cfg<T, S>::Sh;
     __shared__ __align__(128) unsigned char ring[2][Sh::CHUNK];
@@ -310,7 +314,9 @@ wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
     wave::Staging<Sh> st{ring, bar, 0, 0};
     wave::staging_init(st);
     const int64_t row0 = (int64_t)blockIdx.x * Sh::ROWS;
-    if (!wave::wave_tile<T, Sh, SCALED, INT_MUL>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs, stall)) {
+    T* cta_state = state ? state + (int64_t)blockIdx.x * (wave::segment_state_values<Sh>() * Sh::THREADS) : nullptr;
+    if (!wave::wave_tile<T, Sh, SCALED, INT_MUL>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs, stall,
+                                                 c_begin, c_end, cta_state)) {
         if (threadIdx.x == 0) atomicExch(err, 1);
     }
 }
@@ -399,18 +405,19 @@ template <typename T> size_t apply_canonical_table_bytes(int64_t n_loc) { return
 template size_t apply_canonical_table_bytes<double>(int64_t);
 template size_t apply_canonical_table_bytes<float>(int64_t);
 
+// Chunk range of one launch of the wave kernel and the segment state (wave_tile).
+struct Seg {
+    int32_t c_begin = 0, c_end = -1;
+    void* state = nullptr;
+};
+
+// The table of one pass (with the scaled form's recurrence and coefficients).
 template <typename Tsrc, typename T, int S>
-cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t grid_rows,
-                             const int32_t* place, const ApplyPass& pass, void* table, int* err,
-                             cudaStream_t stream, cudaEvent_t ev_begin, cudaEvent_t ev_end, int what)
+cudaError_t prep_pass_shape(const Tsrc* grid, int64_t grid_rows, const int32_t* place, const ApplyPass& pass,
+                            void* table, cudaStream_t stream)
 {
     using Sh = typename Cfg<T, S>::Sh;
-    if (pass.n_loc < 2 || pass.layers <= 0) return cudaSuccess;
-    if (m <= 0 && what != kPassTable) return cudaSuccess;
-    const bool prep = (what & kPassTable) != 0, run = (what & kPassWave) != 0;
     const int64_t n_chunks = Sh::chunks(pass.n_loc);
-    const int64_t blocks = (m + Sh::ROWS - 1) / Sh::ROWS;
-    cudaError_t e;
     if constexpr (sizeof(T) == 8) {
         if (pass.form == 1) {
             unsigned char* tb = (unsigned char*)table;
@@ -419,61 +426,137 @@ cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int
             unsigned char* form = slot + scaled_pre_bytes(pass.n_loc);
             double* dfinal = (double*)(form + scaled_form_bytes(pass.n_loc));
             static_assert(sizeof(Tsrc) == 8, "the scaled form reads an FP64 grid");
-            if (prep) {
-                if (!pass.rec) {  // else launch_scaled_recurrences filled this pass's slot
-                    e = cudaFuncSetAttribute(scaled_recurrence_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RecSmem));
-                    if (e != cudaSuccess) return e;
-                    scaled_recurrence_kernel<<<1, 64, sizeof(RecSmem), stream>>>(
-                        (const double*)grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers, slot,
-                        scaled_slot_bytes(pass.n_loc));
-                }
-                const int64_t total = n_chunks * Sh::CH * Sh::G;
-                int64_t tb_blocks = (total + 255) / 256;
-                if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;
-                scaled_table_kernel<Tsrc, S><<<(unsigned)tb_blocks, 256, 0, stream>>>(
-                    tb, n_chunks, grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers,
-                    pre, form, dfinal);
-                e = cudaGetLastError();
+            if (!pass.rec) {  // else launch_scaled_recurrences filled this pass's slot
+                cudaError_t e = cudaFuncSetAttribute(scaled_recurrence_kernel,
+                                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(RecSmem));
                 if (e != cudaSuccess) return e;
+                scaled_recurrence_kernel<<<1, 64, sizeof(RecSmem), stream>>>(
+                    (const double*)grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers, slot,
+                    scaled_slot_bytes(pass.n_loc));
             }
-            if (!run) return cudaSuccess;
-            if (ev_begin) cudaEventRecord(ev_begin, stream);
-            wave_apply_kernel<T, S, true><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
-                Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
-                (int32_t)n_chunks, err, (T)-0.0, pass.rs, pass.stall > 0 ? pass.stall : 0x7fffffff);
-            e = cudaGetLastError();
-            if (ev_end) cudaEventRecord(ev_end, stream);
-            return e;
+            const int64_t total = n_chunks * Sh::CH * Sh::G;
+            int64_t tb_blocks = (total + 255) / 256;
+            if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;
+            scaled_table_kernel<Tsrc, S><<<(unsigned)tb_blocks, 256, 0, stream>>>(
+                tb, n_chunks, grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0, pass.layers,
+                pre, form, dfinal);
+            return cudaGetLastError();
         }
     }
-    if (prep) {
-        const int64_t total = n_chunks * Sh::CH * Sh::G * Sh::KB;
-        int64_t tb_blocks = (total + 255) / 256;
-        if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;
-        build_table_kernel<Tsrc, T, S><<<(unsigned)tb_blocks, 256, 0, stream>>>(
-            (unsigned char*)table, n_chunks, grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0,
-            pass.layers);
-        e = cudaGetLastError();
+    const int64_t total = n_chunks * Sh::CH * Sh::G * Sh::KB;
+    int64_t tb_blocks = (total + 255) / 256;
+    if (tb_blocks > 152 * 16) tb_blocks = 152 * 16;
+    build_table_kernel<Tsrc, T, S><<<(unsigned)tb_blocks, 256, 0, stream>>>(
+        (unsigned char*)table, n_chunks, grid, grid_rows, place, pass.c0, pass.n_loc, pass.L0,
+        pass.layers);
+    return cudaGetLastError();
+}
+
+// The wave kernel over chunks [seg.c_begin, seg.c_end) of one pass, rows [0, m).
+// `int_mul_rows`: the canonical FP64 form takes the integer-pipe products from this many rows
+// of the launch on.
+template <typename T, int S>
+cudaError_t launch_wave_shape(T* Q, int64_t ldq, int64_t m, const ApplyPass& pass, const void* table, int* err,
+                              cudaStream_t stream, const Seg& seg, int64_t int_mul_rows = kIntMulRows)
+{
+    using Sh = typename Cfg<T, S>::Sh;
+    const int64_t n_chunks = Sh::chunks(pass.n_loc);
+    const int64_t blocks = (m + Sh::ROWS - 1) / Sh::ROWS;
+    const int32_t stall = pass.stall > 0 ? pass.stall : 0x7fffffff;
+    T* q = Q + pass.c0 * ldq;
+    const unsigned char* tb = (const unsigned char*)table;
+    if constexpr (sizeof(T) == 8) {
+        if (pass.form == 1) {
+            wave_apply_kernel<T, S, true><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
+                q, ldq, m, (int32_t)pass.n_loc, tb, (int32_t)n_chunks, err, (T)-0.0, pass.rs, stall,
+                seg.c_begin, seg.c_end, (T*)seg.state);
+            return cudaGetLastError();
+        }
+        if (pass.form == 0 && m >= int_mul_rows) {   // canonical FP64: products on the integer pipes
+            wave_apply_kernel<T, S, false, true><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
+                q, ldq, m, (int32_t)pass.n_loc, tb, (int32_t)n_chunks, err, (T)-0.0, pass.rs, stall,
+                seg.c_begin, seg.c_end, (T*)seg.state);
+            return cudaGetLastError();
+        }
+    }
+    wave_apply_kernel<T, S><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
+        q, ldq, m, (int32_t)pass.n_loc, tb, (int32_t)n_chunks, err, (T)-0.0, pass.rs, stall,
+        seg.c_begin, seg.c_end, (T*)seg.state);
+    return cudaGetLastError();
+}
+
+template <typename Tsrc, typename T, int S>
+cudaError_t apply_pass_shape(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t grid_rows,
+                             const int32_t* place, const ApplyPass& pass, void* table, int* err,
+                             cudaStream_t stream, cudaEvent_t ev_begin, cudaEvent_t ev_end, int what)
+{
+    if (pass.n_loc < 2 || pass.layers <= 0) return cudaSuccess;
+    if (m <= 0 && what != kPassTable) return cudaSuccess;
+    cudaError_t e;
+    if (what & kPassTable) {
+        e = prep_pass_shape<Tsrc, T, S>(grid, grid_rows, place, pass, table, stream);
         if (e != cudaSuccess) return e;
     }
-    if (!run) return cudaSuccess;
+    if (!(what & kPassWave)) return cudaSuccess;
     if (ev_begin) cudaEventRecord(ev_begin, stream);
-    bool int_mul = false;
-    if constexpr (sizeof(T) == 8) {
-        int_mul = pass.form == 0 && m >= kIntMulRows;   // canonical FP64: products on the integer pipes
-        if (int_mul)
-            wave_apply_kernel<T, S, false, true><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
-                Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
-                (int32_t)n_chunks, err, (T)-0.0, pass.rs, pass.stall > 0 ? pass.stall : 0x7fffffff);
-    }
-    if (!int_mul)
-        wave_apply_kernel<T, S><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
-            Q + pass.c0 * ldq, ldq, m, (int32_t)pass.n_loc, (const unsigned char*)table,
-            (int32_t)n_chunks, err, (T)-0.0, pass.rs, pass.stall > 0 ? pass.stall : 0x7fffffff);
-    e = cudaGetLastError();
+    e = launch_wave_shape<T, S>(Q, ldq, m, pass, table, err, stream, Seg{});
     if (ev_end) cudaEventRecord(ev_end, stream);
     return e;
+}
+
+// The host-pointer apply of one pass of k <= 64 layers, streamed by column segments.  The
+// caller's column-major Q (host memory, leading dimension lda) goes to the device buffer dQ
+// (leading dimension m) in column chunks on io.s_in; the pass runs as io.nseg launches over
+// consecutive chunk ranges of its table on `stream`, each waiting for the columns its chunks
+// read (wave_tile: below c_end * CH + W) and carrying its registers to the next launch in
+// io.state; the columns a launch finishes (below c_end * CH - (G-1) * W - KB, all of them after
+// the last) go back on io.s_out as soon as it ends.  So the copies in both directions overlap
+// the kernels, and every launch runs the whole m-row grid (the integer-pipe products and the
+// one-CTA-per-SM shape need all rows together).  Only stream events order the three streams.
+template <typename T, int S>
+cudaError_t host_segmented_shape(T* dQ, int64_t m, const T* d_cs, const ApplyPass& pass, void* table, int* err,
+                                 cudaStream_t stream, const HostStream& io)
+{
+    using Sh = typename Cfg<T, S>::Sh;
+    const int64_t n = pass.n_loc;
+    cudaError_t e = prep_pass_shape<T, T, S>(d_cs, n - 1, nullptr, pass, table, stream);
+    if (e != cudaSuccess) return e;
+    const int64_t n_chunks = Sh::chunks(n);
+    const int nseg = (int)std::max<int64_t>(1, std::min<int64_t>(io.nseg, n_chunks));
+    const size_t esz = sizeof(T);
+    T* host = (T*)io.host;
+    int64_t in_lo = 0, out_lo = 0;
+    // copies in and kernels first, then the copies out: with pageable host memory a copy out
+    // blocks the calling thread until it is done, and must not hold back the next copy in
+    for (int j = 0; j < nseg; ++j) {
+        const int64_t cb = (int64_t)j * n_chunks / nseg, ce = (int64_t)(j + 1) * n_chunks / nseg;
+        const int64_t in_hi = std::min<int64_t>(n, ce * Sh::CH + Sh::W);
+        if (in_hi > in_lo) {
+            e = cudaMemcpy2DAsync(dQ + in_lo * m, m * esz, host + in_lo * io.lda, io.lda * esz, m * esz,
+                                  in_hi - in_lo, cudaMemcpyHostToDevice, io.s_in);
+            if (e != cudaSuccess) return e;
+            in_lo = in_hi;
+        }
+        if ((e = cudaEventRecord(io.ev_in[j], io.s_in)) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(stream, io.ev_in[j], 0)) != cudaSuccess) return e;
+        Seg seg{(int32_t)cb, (int32_t)ce, io.state};
+        e = launch_wave_shape<T, S>(dQ, m, m, pass, table, err, stream, seg, 0);
+        if (e != cudaSuccess) return e;
+        if ((e = cudaEventRecord(io.ev_seg[j], stream)) != cudaSuccess) return e;
+    }
+    for (int j = 0; j < nseg; ++j) {
+        const int64_t ce = (int64_t)(j + 1) * n_chunks / nseg;
+        const int64_t out_hi = (j == nseg - 1) ? n
+            : std::max<int64_t>(0, std::min<int64_t>(n, ce * Sh::CH - (int64_t)(Sh::G - 1) * Sh::W - Sh::KB));
+        if ((e = cudaStreamWaitEvent(io.s_out, io.ev_seg[j], 0)) != cudaSuccess) return e;
+        if (out_hi > out_lo) {
+            e = cudaMemcpy2DAsync(host + out_lo * io.lda, io.lda * esz, dQ + out_lo * m, m * esz, m * esz,
+                                  out_hi - out_lo, cudaMemcpyDeviceToHost, io.s_out);
+            if (e != cudaSuccess) return e;
+            out_lo = out_hi;
+        }
+    }
+    return cudaSuccess;
 }
 
 template <typename Tsrc, typename T>
@@ -502,6 +585,45 @@ cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t g
     return apply_pass_shape<Tsrc, T, 1>(Q, ldq, m, grid, grid_rows, place, pass, table, err, stream,
                                         ev_begin, ev_end, what);
 }
+
+template <typename T>
+cudaError_t apply_host_segmented(T* dQ, int64_t m, const T* d_cs, const ApplyPass& pass, void* table, int* err,
+                                 cudaStream_t stream, const HostStream& io)
+{
+    if (pass.n_loc < 2 || pass.layers <= 0 || m <= 0) return cudaSuccess;
+    if (pass.layers > 64 || pass.c0 != 0 || pass.L0 != 0) return cudaErrorInvalidValue;
+    const int s = shape_index<T>();
+    if constexpr (sizeof(T) == 8) {
+        if (s == 2 || (s == 0 && m >= kWideRows))
+            return host_segmented_shape<T, 2>(dQ, m, d_cs, pass, table, err, stream, io);
+    }
+    if constexpr (sizeof(T) == 4) {
+        if (s == 2) return host_segmented_shape<T, 2>(dQ, m, d_cs, pass, table, err, stream, io);
+        if (s == 3) return host_segmented_shape<T, 3>(dQ, m, d_cs, pass, table, err, stream, io);
+    }
+    if (s == 0) return host_segmented_shape<T, 0>(dQ, m, d_cs, pass, table, err, stream, io);
+    return host_segmented_shape<T, 1>(dQ, m, d_cs, pass, table, err, stream, io);
+}
+template cudaError_t apply_host_segmented<double>(double*, int64_t, const double*, const ApplyPass&, void*, int*,
+                                                  cudaStream_t, const HostStream&);
+template cudaError_t apply_host_segmented<float>(float*, int64_t, const float*, const ApplyPass&, void*, int*,
+                                                 cudaStream_t, const HostStream&);
+
+// Device memory the segment state of an m-row launch needs (the largest over the shapes).
+template <typename T, int S> size_t state_bytes(int64_t m)
+{
+    using Sh = typename Cfg<T, S>::Sh;
+    return (size_t)((m + Sh::ROWS - 1) / Sh::ROWS) * Sh::THREADS * wave::segment_state_values<Sh>() * sizeof(T);
+}
+template <typename T> size_t apply_segment_state_bytes(int64_t m)
+{
+    size_t b = std::max(state_bytes<T, 0>(m), state_bytes<T, 1>(m));
+    b = std::max(b, state_bytes<T, 2>(m));
+    if constexpr (sizeof(T) == 4) b = std::max(b, state_bytes<T, 3>(m));
+    return b;
+}
+template size_t apply_segment_state_bytes<double>(int64_t);
+template size_t apply_segment_state_bytes<float>(int64_t);
 
 int apply_num_shapes(int fp64) { return kShapes[fp64 ? 0 : 1]; }
 void apply_set_shape(int fp64, int shape)

@@ -158,6 +158,25 @@ cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t g
                        cudaStream_t stream, cudaEvent_t ev_begin = nullptr,
                        cudaEvent_t ev_end = nullptr, int what = kPassAll);
 
+// A host-resident Q streamed through the device by column segments (apply_host_segmented).
+struct HostStream {
+    void* host;             // the caller's m x n column-major matrix (host memory)
+    int64_t lda;            // its leading dimension
+    cudaStream_t s_in, s_out;
+    cudaEvent_t* ev_in;     // nseg events: columns of segment j copied in
+    cudaEvent_t* ev_seg;    // nseg events: segment j's kernel done
+    int nseg;
+    void* state;            // apply_segment_state_bytes(m) bytes of device memory
+};
+
+// One pass of k <= 64 layers of the (n-1) x k grid d_cs (Julia layout, on the device) applied
+// to a host-resident m x n Q through the device buffer dQ (leading dimension m), with the
+// copies in, the kernels and the copies out overlapped by column segments (see apply.cu).
+template <typename T>
+cudaError_t apply_host_segmented(T* dQ, int64_t m, const T* d_cs, const ApplyPass& pass, void* table, int* err,
+                                 cudaStream_t stream, const HostStream& io);
+template <typename T> size_t apply_segment_state_bytes(int64_t m);
+
 // Tile shape of the single-matrix wave kernel per precision (see apply.cu).
 void apply_set_shape(int fp64, int shape);
 int apply_get_shape(int fp64);

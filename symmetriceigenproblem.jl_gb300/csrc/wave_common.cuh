@@ -252,9 +252,21 @@ __device__ __forceinline__ void staging_init(Staging<Sh>& st)
     __syncthreads();
 }
 
+// Values a thread carries across a segment boundary (see wave_tile): its windows, its ring of
+// columns read ahead, and the column it last handed to the next lane group.
+template <typename Sh> __host__ __device__ constexpr int segment_state_values() { return Sh::R * (2 * Sh::W + 1); }
+
 // One tile: rows [row0, row0 + ROWS) of Q (m rows, columns [0, n_loc) of the pass) through
-// the n_chunks chunks of `table`.  `stall` (a test hook, default never): chunks from that
-// index on are not copied, so their bounded waits run out and the tile returns false.
+// chunks [c_begin, c_end) of the n_chunks chunks of `table` (c_end < 0: to the last).
+// A pass may run as several launches over consecutive chunk ranges ("segments"): a segment
+// that does not start at chunk 0 restores each thread's registers from `state` (which the
+// previous segment saved there), and one that does not end at the last chunk saves them.
+// Chunk c reads the columns below (c + 1) * CH + W and finishes the columns below
+// (c + 1) * CH - (G - 1) * W - KB, so a segment needs only the columns its chunks read, and
+// the columns it finishes are final.  `state` (segments only) points at this CTA's
+// segment_state_values * THREADS values, laid out value-major so that saving and restoring
+// are coalesced.  `stall` (a test hook, default never): chunks from that index on are not
+// copied, so their bounded waits run out and the tile returns false.
 // Element (row, col) is Q[row * rs + col * ldq]: rs = 1 for
 // the column rotations of rmul! on a column-major matrix, rs = lda and ldq = 1 for the row
 // rotations of lmul! (the same wave on the transposed view).  Every thread of the CTA calls
@@ -263,14 +275,19 @@ template <typename T, typename Sh, bool SCALED = false, bool INT_MUL = false>
 __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_t m, int64_t row0,
                                           int32_t n_loc, const unsigned char* __restrict__ table,
                                           int32_t n_chunks, const T nz, Staging<Sh>& st,
-                                          int64_t rs = 1, int32_t stall = 0x7fffffff)
+                                          int64_t rs = 1, int32_t stall = 0x7fffffff,
+                                          int32_t c_begin = 0, int32_t c_end = -1,
+                                          T* __restrict__ state = nullptr)
 {
     constexpr int KB = Sh::KB, G = Sh::G, CH = Sh::CH, W = Sh::W, RPW = Sh::RPW, R = Sh::R;
     const int tid = threadIdx.x;
+    if (c_end < 0 || c_end > n_chunks) c_end = n_chunks;
     if (tid == 0) {
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        bulk_load(st.ring[0], table, Sh::CHUNK, &st.bar[0]);
-        if (n_chunks > 1 && stall > 1) bulk_load(st.ring[1], table + Sh::CHUNK, Sh::CHUNK, &st.bar[1]);
+        if (c_begin < c_end && c_begin < stall)
+            bulk_load(st.ring[0], table + (int64_t)c_begin * Sh::CHUNK, Sh::CHUNK, &st.bar[0]);
+        if (c_begin + 1 < c_end && c_begin + 1 < stall)
+            bulk_load(st.ring[1], table + (int64_t)(c_begin + 1) * Sh::CHUNK, Sh::CHUNK, &st.bar[1]);
     }
 
     // lane rl of group g holds rows rbase + r*RPW, r < R, of the warp's R*RPW rows
@@ -290,21 +307,33 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
     const int lag = g * W;  // waves this group trails group 0
 
     T win[R][W], ahead[R][W];
+    T xout[R];
+    constexpr int NT = Sh::THREADS;
+    if (c_begin == 0) {
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
+        for (int r = 0; r < R; ++r) {
 #pragma unroll
-        for (int q = 0; q < W; ++q) {
-            win[r][q] = T(0);
-            ahead[r][q] = (q < n_loc) ? qrow[r][(int64_t)q * ldq] : T(0);
+            for (int q = 0; q < W; ++q) {
+                win[r][q] = T(0);
+                ahead[r][q] = (q < n_loc) ? qrow[r][(int64_t)q * ldq] : T(0);
+            }
+            xout[r] = T(0);
+        }
+    } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+#pragma unroll
+            for (int q = 0; q < W; ++q) {
+                win[r][q] = state[(r * (2 * W + 1) + q) * NT + tid];
+                ahead[r][q] = state[(r * (2 * W + 1) + W + q) * NT + tid];
+            }
+            xout[r] = state[(r * (2 * W + 1) + 2 * W) * NT + tid];
         }
     }
-    T xout[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) xout[r] = T(0);
 
-    for (int32_t c = 0; c < n_chunks; ++c) {
-        const int b = c & 1;
-        const uint32_t parity = ((b ? st.uses1 : st.uses0) + (uint32_t)(c >> 1)) & 1u;
+    for (int32_t c = c_begin; c < c_end; ++c) {
+        const int b = (c - c_begin) & 1;
+        const uint32_t parity = ((b ? st.uses1 : st.uses0) + (uint32_t)((c - c_begin) >> 1)) & 1u;
         const bool ok = mbar_wait_bounded(&st.bar[b], parity);
         if (__syncthreads_or(!ok)) return false;
         const unsigned char* sb = st.ring[b] + g * Sh::GSTRIDE;
@@ -375,13 +404,25 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
             }
         }
         __syncthreads();
-        if (tid == 0 && c + 2 < n_chunks && c + 2 < stall) {
+        if (tid == 0 && c + 2 < c_end && c + 2 < stall) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             bulk_load(st.ring[b], table + (int64_t)(c + 2) * Sh::CHUNK, Sh::CHUNK, &st.bar[b]);
         }
     }
-    st.uses0 += (uint32_t)((n_chunks + 1) >> 1);
-    st.uses1 += (uint32_t)(n_chunks >> 1);
+    const int32_t used = c_end > c_begin ? c_end - c_begin : 0;
+    st.uses0 += (uint32_t)((used + 1) >> 1);
+    st.uses1 += (uint32_t)(used >> 1);
+    if (state != nullptr && c_end < n_chunks) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+#pragma unroll
+            for (int q = 0; q < W; ++q) {
+                state[(r * (2 * W + 1) + q) * NT + tid] = win[r][q];
+                state[(r * (2 * W + 1) + W + q) * NT + tid] = ahead[r][q];
+            }
+            state[(r * (2 * W + 1) + 2 * W) * NT + tid] = xout[r];
+        }
+    }
     return true;
 }
 

@@ -48,11 +48,15 @@ def test_apply_host_buffers_with_leading_dimension(cuda, pkg, oracle, dtype):
 
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("m,n,k,ld", [(4100, 300, 64, 4100), (4099, 129, 40, 4111), (4096, 70, 1, 4096),
-                                      (5000, 200, 65, 5000), (2100, 90, 64, 2100)])
-def test_apply_host_pipelined_row_blocks(cuda, pkg, oracle, m, n, k, ld, dtype):
-    """Host Q with k <= 64 and m >= 4096 runs as 16 row blocks on 16 streams (copy in, kernel,
-    copy out each), all sharing one table; the result is the oracle's bits, the rows beyond m
-    of a leading dimension are untouched.  k = 65 and m = 2100 take the unpipelined path."""
+                                      (5000, 200, 65, 5000), (2100, 90, 64, 2100), (4096, 2001, 64, 4096),
+                                      (15360, 600, 64, 15363), (4097, 3, 2, 4097), (4096, 2, 64, 4096)])
+def test_apply_host_pipelined_column_segments(cuda, pkg, oracle, m, n, k, ld, dtype):
+    """Host Q with k <= 64 and m >= 4096 runs as 16 launches over column segments of one pass
+    (copies in, kernels and copies out on three streams; each launch carries its registers to
+    the next through a state buffer): the result is the oracle's bits, and the rows beyond m of
+    a leading dimension are untouched.  Small n gives one table chunk per segment (every
+    boundary a segment boundary); m = 15360 takes the 27-warp FP64 shape.  k = 65 and
+    m = 2100 take the unpipelined path."""
     rng = np.random.default_rng(m + n + k)
     big = np.asfortranarray((rng.random((ld, n)) * 2 - 1).astype(dtype))
     A = big[:m, :]

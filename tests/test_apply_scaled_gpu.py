@@ -77,3 +77,16 @@ def test_qr_scaled_apply_matches_oracle(cuda, pkg, oracle, exact, n, seed):
         T = np.diag(d) + np.diag(e, 1) + np.diag(e, -1)
         assert np.linalg.norm(T @ Q - Q * H.dv) / np.linalg.norm(T) <= 10 * n * EPS
         assert np.linalg.norm(Q.T @ Q - np.eye(n)) <= 10 * n * EPS
+
+
+@pytest.mark.parametrize("m,n,k", [(4096, 300, 64), (4100, 77, 33)])
+def test_scaled_apply_host_pipelined(cuda, pkg, oracle, m, n, k):
+    """The scaled form through the host-pointer entry point, which streams Q by column segments
+    (m >= 4096, k <= 64): the oracle's restatement of the form, bit for bit."""
+    rng = np.random.default_rng(m + n + k)
+    g = rotation_grid(pkg, rng, n, k)
+    A = np.asfortranarray(rng.random((m, n)) * 2 - 1)
+    ref = A.copy(order="F")
+    oracle.apply_scaled(ref, g)
+    pkg.bulk_wave_order_2x2_rmul_(A, g, form=1)
+    assert np.array_equal(A, ref)
