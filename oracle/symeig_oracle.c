@@ -506,6 +506,7 @@ typedef struct {
     int64_t min_from, max_to;   /* 1-based column range of the last flush's sweeps */
     int32_t ms_bulges;          /* multishift batches: bulge cap (0: single shifts only) */
     int32_t ms_rows;            /* multishift batches: block rows per bulge */
+    int32_t ms_window;          /* multishift batches: shift window, in multiples of the bulges */
     int64_t batches;            /* multishift batches run */
 } oracle_qr_state;
 
@@ -519,44 +520,66 @@ void oracle_qr_init(oracle_qr_state* st, int64_t n, int32_t max_layers, double t
     st->grid_layers = exact_order ? 2 * max_layers : max_layers;
 }
 
-/* The eigenvalues of the trailing nb x nb principal submatrix of a block ending at row `to`
- * (1-based), ascending: bisection on Sturm counts (the LDL^T pivots of T - x I, a negative
- * pivot per eigenvalue below x) down to adjacent doubles.  They are the shifts of a multishift
- * batch.  The device computes the same eigenvalues to about 1e-16 relative to the block's
- * norm by FP32 bisection and FP64 Newton steps; shifts only steer convergence, so the two
- * need not agree in their last bits. */
-static void oracle_trailing_eigenvalues(const double* dv, const double* ev, int64_t to, int nb, double* out)
+/* The shifts of a multishift batch of nb sweeps over the block [from, to] (1-based): nb
+ * eigenvalues of the block's trailing w x w principal submatrix, w = min(window * nb, to -
+ * from + 1), ascending -- those ranked about the bottom diagonal entry: with r the number of
+ * the window's eigenvalues below dv[to] (a Sturm count), the ones of rank k0 .. k0 + nb - 1,
+ * k0 = min(max(r - nb / 2, 0), w - nb).  With window = 1 they are all of the trailing
+ * square's eigenvalues.  A window twice the batch approximates the eigenvalues that belong
+ * to the bottom rows better than the square of the batch's size does (about a quarter fewer
+ * sweeps at n = 16384, case A).  Eigenvalues by bisection on Sturm counts (the LDL^T pivots of
+ * T - x I, a negative pivot per eigenvalue below x) down to adjacent doubles.  The device
+ * computes the same eigenvalues to about 1e-16 relative to the window's norm by FP32
+ * bisection and a safeguarded FP64 Newton iteration; shifts only steer convergence, so the
+ * two need not agree in their last bits. */
+static int oracle_sturm_count(const double* d, const double* e, int w, double x, double pivmin)
 {
-    const double* d = dv + (to - nb);
-    const double* e = ev + (to - nb);
+    int cnt = 0;
+    double q = d[0] - x;
+    if (q < 0.0) ++cnt;
+    for (int i = 1; i < w; ++i) {
+        if (fabs(q) < pivmin) q = -pivmin;
+        q = (d[i] - x) - e[i - 1] * e[i - 1] / q;
+        if (q < 0.0) ++cnt;
+    }
+    return cnt;
+}
+
+static void oracle_trailing_eigenvalues(const double* dv, const double* ev, int64_t from, int64_t to, int nb,
+                                        int window, double* out)
+{
+    int64_t w64 = (int64_t)window * nb;
+    if (w64 > to - from + 1) w64 = to - from + 1;
+    const int w = (int)w64;
+    const double* d = dv + (to - w);
+    const double* e = ev + (to - w);
     double lo = INFINITY, hi = -INFINITY, e2max = 0.0;
-    for (int i = 0; i < nb; ++i) {
-        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < nb - 1 ? fabs(e[i]) : 0.0);
+    for (int i = 0; i < w; ++i) {
+        const double r = (i > 0 ? fabs(e[i - 1]) : 0.0) + (i < w - 1 ? fabs(e[i]) : 0.0);
         if (d[i] - r < lo) lo = d[i] - r;
         if (d[i] + r > hi) hi = d[i] + r;
-        if (i < nb - 1 && e[i] * e[i] > e2max) e2max = e[i] * e[i];
+        if (i < w - 1 && e[i] * e[i] > e2max) e2max = e[i] * e[i];
     }
     const double pivmin = DBL_MIN * (e2max > 1.0 ? e2max : 1.0);
-    const double w = hi - lo;
-    lo -= 1e-12 * (w > 0.0 ? w : 1.0) + DBL_MIN;
-    hi += 1e-12 * (w > 0.0 ? w : 1.0) + DBL_MIN;
-    for (int k = 0; k < nb; ++k) {
+    const double wd = hi - lo;
+    lo -= 1e-12 * (wd > 0.0 ? wd : 1.0) + DBL_MIN;
+    hi += 1e-12 * (wd > 0.0 ? wd : 1.0) + DBL_MIN;
+    int k0 = 0;
+    if (w > nb) {
+        k0 = oracle_sturm_count(d, e, w, d[w - 1], pivmin) - nb / 2;
+        if (k0 < 0) k0 = 0;
+        if (k0 > w - nb) k0 = w - nb;
+    }
+    for (int j = 0; j < nb; ++j) {
+        const int k = k0 + j;
         double a = lo, b = hi;
         for (int it = 0; it < 200; ++it) {
             const double mid = 0.5 * (a + b);
             if (!(mid > a && mid < b)) break;
-            int cnt = 0;
-            double q = d[0] - mid;
-            if (q < 0.0) ++cnt;
-            for (int i = 1; i < nb; ++i) {
-                if (fabs(q) < pivmin) q = -pivmin;
-                q = (d[i] - mid) - e[i - 1] * e[i - 1] / q;
-                if (q < 0.0) ++cnt;
-            }
-            if (cnt > k) b = mid;
+            if (oracle_sturm_count(d, e, w, mid, pivmin) > k) b = mid;
             else a = mid;
         }
-        out[k] = 0.5 * (a + b);
+        out[j] = 0.5 * (a + b);
     }
 }
 
@@ -615,7 +638,7 @@ int oracle_qr_flush(oracle_qr_state* st, double* dv, double* ev, double* givens,
                 did_a_thing = 1;
                 if (nbl >= 2) {
                     double shifts[128];
-                    oracle_trailing_eigenvalues(dv, ev, to, (int)nbl, shifts);
+                    oracle_trailing_eigenvalues(dv, ev, from, to, (int)nbl, st->ms_window, shifts);
                     for (int64_t j = 0; j < nbl; ++j)
                         oracle_single_shift(dv, ev, n, from, to, shifts[j], givens, rows, thick, place,
                                             layer > 0 ? layer + j : 0);
@@ -665,8 +688,9 @@ int oracle_qr(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, 
  * as the device applies it. */
 static int oracle_qr_driver(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
                             int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
-                            int32_t apply_form, int32_t ms_bulges, int32_t ms_rows, int32_t* converged,
-                            int64_t* iter, int64_t* flushes, int64_t* rotations, int64_t* batches);
+                            int32_t apply_form, int32_t ms_bulges, int32_t ms_rows, int32_t ms_window,
+                            int32_t* converged, int64_t* iter, int64_t* flushes, int64_t* rotations,
+                            int64_t* batches);
 
 int oracle_qr_form(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
                    int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
@@ -674,29 +698,31 @@ int oracle_qr_form(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_
                    int64_t* rotations)
 {
     return oracle_qr_driver(d, e, n, Q, ldq, m, q_is_f32, max_layers, tol, maxiter, exact_order,
-                            apply_form, 0, 16, converged, iter, flushes, rotations, NULL);
+                            apply_form, 0, 16, 1, converged, iter, flushes, rotations, NULL);
 }
 
 /* The device's multishift chase (chase mode 3; not the reference's algorithm, which is
  * oracle_qr) restated: where a block has room, a batch of up to ms_bulges sweeps
  * (min(ms_bulges, len / ms_rows), the layer room and maxiter decide) with the eigenvalues of
- * the block's trailing square as shifts, run as sweeps in sequence with the reference's
- * rotations; every other decision, the apply and the placement as in oracle_qr.  FP64 Q,
- * canonical apply.  *batches receives the number of batches. */
+ * a trailing window of ms_window times the batch's size as shifts (oracle_trailing_eigenvalues),
+ * run as sweeps in sequence with the reference's rotations; every other decision, the apply
+ * and the placement as in oracle_qr.  FP64 Q, canonical apply.  *batches receives the number
+ * of batches. */
 int oracle_qr_multishift(double* d, double* e, int64_t n, double* Q, int64_t ldq, int64_t m,
                          int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
-                         int32_t ms_bulges, int32_t ms_rows, int32_t* converged, int64_t* iter,
-                         int64_t* flushes, int64_t* rotations, int64_t* batches)
+                         int32_t ms_bulges, int32_t ms_rows, int32_t ms_window, int32_t* converged,
+                         int64_t* iter, int64_t* flushes, int64_t* rotations, int64_t* batches)
 {
-    if (ms_bulges < 2 || ms_bulges > 128 || ms_rows < 4) return 1;
+    if (ms_bulges < 2 || ms_bulges > 128 || ms_rows < 4 || ms_window < 1 || ms_window > 4) return 1;
     return oracle_qr_driver(d, e, n, Q, ldq, m, 0, max_layers, tol, maxiter, exact_order, 0, ms_bulges,
-                            ms_rows, converged, iter, flushes, rotations, batches);
+                            ms_rows, ms_window, converged, iter, flushes, rotations, batches);
 }
 
 static int oracle_qr_driver(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
                             int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
-                            int32_t apply_form, int32_t ms_bulges, int32_t ms_rows, int32_t* converged,
-                            int64_t* iter, int64_t* flushes, int64_t* rotations, int64_t* batches)
+                            int32_t apply_form, int32_t ms_bulges, int32_t ms_rows, int32_t ms_window,
+                            int32_t* converged, int64_t* iter, int64_t* flushes, int64_t* rotations,
+                            int64_t* batches)
 {
     if (apply_form != 0 && q_is_f32) return 1;
     if (n < 1 || max_layers < 1 || (Q && ldq < m)) return 1;
@@ -704,6 +730,7 @@ static int oracle_qr_driver(double* d, double* e, int64_t n, void* Q, int64_t ld
     oracle_qr_init(&st, n, max_layers, tol, maxiter, exact_order);
     st.ms_bulges = ms_bulges;
     st.ms_rows = ms_rows;
+    st.ms_window = ms_window;
     int64_t nr = n > 1 ? n - 1 : 1;
     int64_t GL = st.grid_layers;
     double* givens = (double*)malloc(sizeof(double) * 2 * nr * GL);
