@@ -80,14 +80,16 @@ int symeig_set_exact_order(symeig_handle h, int32_t exact_order);
  * 1: the reference form (correctly rounded division and square root) on one thread.
  * 2: as 0, but every sweep is then redone in the reference form (exercises the restore).
  * 3: multishift.  Where a block has at least 2 * 16 rows and room for several layers, the
- *   chase runs a batch of up to 64 sweeps (symeig_set_multishift) whose shifts are the
- *   eigenvalues of the block's trailing square (one per sweep), as bulges chased
- *   concurrently on separate SMs, each a fixed number of rows behind the one before.  The deflation test, the capacity rule and
- *   the rotation placement are those of a sequence of single sweeps with those shifts; shorter
- *   blocks take the Wilkinson single sweep of mode 0.  Results meet the same error bounds as
- *   the reference (eigenvalues within 10 n eps ||T||, residual and orthogonality within
- *   10 n eps) but are not the reference's bits; the sweep count is higher (about 1.2-1.6x),
- *   the chase time far lower.  No reference counterpart. */
+ *   chase runs a batch of up to 64 sweeps (symeig_set_multishift) whose shifts are nb
+ *   eigenvalues of the block's trailing window of 2 nb rows (those ranked about its bottom
+ *   entry; FP32 bisection, then a safeguarded FP64 Newton iteration), as bulges chased
+ *   concurrently on separate SMs, each a fixed number of rows behind the one before.  The
+ *   deflation test, the capacity rule and the rotation placement are those of a sequence of
+ *   single sweeps with those shifts; shorter blocks take the Wilkinson single sweep of mode 0.
+ *   Results meet the same error bounds as the reference (eigenvalues within 10 n eps ||T||,
+ *   residual and orthogonality within 10 n eps) but are not the reference's bits; the sweep
+ *   count is about the reference's (1.00x at n = 16384 with d_i = i, about 1.3x on a random
+ *   diagonal), the chase time far lower.  No reference counterpart. */
 int symeig_set_chase_mode(symeig_handle h, int32_t mode);
 /* Batch shape of chase mode 3: a batch over a block of len rows runs
  * min(max_bulges, len / rows_per_bulge) bulges (and only when that is at least 2), and each
@@ -97,12 +99,15 @@ int symeig_set_chase_mode(symeig_handle h, int32_t mode);
 int symeig_set_multishift(symeig_handle h, int32_t max_bulges, int32_t rows_per_bulge,
                           int32_t release_every);
 /* Arithmetic form of the FP64 bulk apply (symeig_apply_givens_f64*, and the qr driver's
- * apply with FP64 Q).  0 (default): every rotation as the reference's rmul!, four FP64
- * operations per rotation and row.  1: the scaled ("fast Givens") form: columns carry scale
- * factors within each pass of 64 layers, so a rotation costs two FMAs per row; results agree
- * with form 0 to a few ulps per rotation (not bit for bit) and with the oracle's restatement
- * of the same form bit for bit.  The FP32, left, batched and allocation-free applies always
- * use form 0.  No reference counterpart. */
+ * apply with FP64 Q).  0 (default): every rotation as the reference's rmul!, two products and
+ * two FMAs per rotation and row; from 3072 rows of Q on, the two products are computed on the
+ * integer pipes (exact round-to-nearest-even FP64 products, see symeig_mul_rn_f64_dev) and
+ * only the FMAs use the FP64 pipe.  2: the same rotation with all four operations on the FP64
+ * pipe; forms 0 and 2 give the same bits.  1: the scaled ("fast Givens") form: columns carry
+ * scale factors within each pass of 64 layers, so a rotation costs two FMAs per row; results
+ * agree with form 0 to a few ulps per rotation (not bit for bit) and with the oracle's
+ * restatement of the same form bit for bit.  The FP32, left, batched and allocation-free
+ * applies use form 0.  No reference counterpart. */
 int symeig_set_apply_form(symeig_handle h, int32_t form);
 /* Test hook for the failure path of the bounded device waits: with chunk > 0 the wave
  * kernels stop copying their rotation table from that chunk on, so their waits run out
@@ -197,9 +202,11 @@ int symeig_qr_batched_f64_dev(symeig_handle h, int64_t count, const int64_t* n, 
 int symeig_batched_autotune(symeig_handle h, double* ms);
 /* Read (set = 0) or write (set != 0) the tile shape of the single-matrix wave kernel for FP64
  * (fp64 != 0) or FP32: 0 = 8 lane groups of 8 layers (4 rows per warp), 1 = 4 groups of 16
- * layers (8 rows per warp); FP32 only: 2 = shape 1 and 3 = shape 0 with two rows per thread;
- * FP64 only: 2 = shape 0 in CTAs of 27 warps (108 rows, one CTA per SM at m = 16384); FP64
- * shape 0 itself runs as 2 when m >= 15000.  Defaults: FP64 0, FP32 2.  Returns SYMEIG_ERR_SIZE for a shape the precision lacks.
+ * layers (8 rows per warp); FP32 only: 2 = shape 1 and 3 = shape 0 with two rows per thread,
+ * 4 = shape 1 in CTAs of 14 warps (112 rows); FP64 only: 2 = shape 0 in CTAs of 27 warps
+ * (108 rows, one CTA per SM at m = 16384).  FP64 shape 0 runs as 2, and FP32 shape 2 as 4,
+ * when m >= 15000.  Defaults: FP64 0, FP32 2.  Returns SYMEIG_ERR_SIZE for a shape the
+ * precision lacks.
  * Process-wide.  No reference counterpart. */
 int symeig_apply_tuning(int32_t fp64, int32_t* shape, int32_t set);
 /* Read (set = 0) or write (set != 0) the batched tuning: class split and shape per class. */

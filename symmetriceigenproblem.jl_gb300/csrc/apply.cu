@@ -30,7 +30,8 @@ using wave::kThreads;
 //             shared memory serves two rows, so the shared-memory pipe (2 wavefronts per
 //             128-bit broadcast read of 4 or 8 distinct addresses) carries half the load per
 //             rotation-row, and each thread has two independent rotation chains.  Shape 2
-//             is the FP32 choice (1.5-3 % ahead of shape 1, measured).
+//             is the FP32 choice (1.5-3 % ahead of shape 1, measured); from 15000 rows on it
+//             runs as shape 4 (below).
 template <typename T, int S> struct Cfg;
 // MINB: CTAs per SM the launch bounds ask for; MINB_INT the same for the FP64 kernels whose
 // products run on the integer pipes (int_mul.cuh: about 95 registers with one row per thread).
@@ -44,12 +45,19 @@ template <> struct Cfg<float, 2> { using Sh = Shape<float, 16, 4, 2>; static con
 // 40 with 6 (the kernel's time is the busiest SM's).  27 warps x 72 registers fit one SM.
 template <> struct Cfg<double, 2> { using Sh = Shape<double, 8, 8, 1, 27>; static constexpr int MINB = 1, MINB_INT = 1; static constexpr int THREADS = Sh::THREADS; };
 template <> struct Cfg<float, 3> { using Sh = Shape<float, 8, 8, 2>; static constexpr int MINB = 4, MINB_INT = 4; static constexpr int THREADS = Sh::THREADS; };
+// FP32 shape 4 = shape 1 (one row per thread) in CTAs of 14 warps (112 rows): at m = 16384,
+// 147 CTAs, about one per SM, 13.5 warps per SM.  FP32 shape 2 runs as shape 4 from 15000
+// rows on: 27.8 TFLOP/s against 25.2 for shape 2 at 16384 x 16384, k = 64 (measured with every other FP32 shape: 8 x 8 in
+// CTAs of 27 warps 25.2, 8 x 8 with two rows per thread in 14 warps 24.9, four rows per
+// thread in 7 warps 24.3, 16 x 4 with two rows in 7 warps 27.6).
+template <> struct Cfg<float, 4> { using Sh = Shape<float, 16, 4, 1, 14>; static constexpr int MINB = 1, MINB_INT = 1; static constexpr int THREADS = Sh::THREADS; };
+static_assert(Cfg<float, 4>::Sh::CHUNK == Cfg<float, 1>::Sh::CHUNK, "table layout");
 // the table depends on (KB, G) only, so shapes 2 and 3 share the tables of 1 and 0
 static_assert(Cfg<float, 2>::Sh::CHUNK == Cfg<float, 1>::Sh::CHUNK, "table layout");
 static_assert(Cfg<float, 3>::Sh::CHUNK == Cfg<float, 0>::Sh::CHUNK, "table layout");
 static_assert(Cfg<double, 2>::Sh::CHUNK == Cfg<double, 0>::Sh::CHUNK, "table layout");
 
-constexpr int kShapes[2] = {3, 4};  // shapes available to [0] FP64, [1] FP32
+constexpr int kShapes[2] = {3, 5};  // shapes available to [0] FP64, [1] FP32
 // FP64 shape 0 runs as shape 2 from this many rows on (about 152 SMs x 108 rows x 0.92)
 constexpr int64_t kWideRows = 15000;
 // The canonical FP64 form computes its products on the integer pipes from this many rows on.
@@ -572,6 +580,9 @@ cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t g
                                                 stream, ev_begin, ev_end, what);
     }
     if constexpr (sizeof(T) == 4) {
+        if (s == 4 || (s == 2 && m >= kWideRows))
+            return apply_pass_shape<Tsrc, T, 4>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
+                                                stream, ev_begin, ev_end, what);
         if (s == 2)
             return apply_pass_shape<Tsrc, T, 2>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
                                                 stream, ev_begin, ev_end, what);
@@ -598,6 +609,7 @@ cudaError_t apply_host_segmented(T* dQ, int64_t m, const T* d_cs, const ApplyPas
             return host_segmented_shape<T, 2>(dQ, m, d_cs, pass, table, err, stream, io);
     }
     if constexpr (sizeof(T) == 4) {
+        if (s == 4 || (s == 2 && m >= kWideRows)) return host_segmented_shape<T, 4>(dQ, m, d_cs, pass, table, err, stream, io);
         if (s == 2) return host_segmented_shape<T, 2>(dQ, m, d_cs, pass, table, err, stream, io);
         if (s == 3) return host_segmented_shape<T, 3>(dQ, m, d_cs, pass, table, err, stream, io);
     }
@@ -619,7 +631,10 @@ template <typename T> size_t apply_segment_state_bytes(int64_t m)
 {
     size_t b = std::max(state_bytes<T, 0>(m), state_bytes<T, 1>(m));
     b = std::max(b, state_bytes<T, 2>(m));
-    if constexpr (sizeof(T) == 4) b = std::max(b, state_bytes<T, 3>(m));
+    if constexpr (sizeof(T) == 4) {
+        b = std::max(b, state_bytes<T, 3>(m));
+        b = std::max(b, state_bytes<T, 4>(m));
+    }
     return b;
 }
 template size_t apply_segment_state_bytes<double>(int64_t);

@@ -113,11 +113,11 @@ def test_left_apply_matches_oracle(cuda, pkg, oracle, m, n, k, dtype):
 
 
 @pytest.mark.parametrize("dtype,shape", [(np.float64, 0), (np.float64, 1), (np.float64, 2), (np.float32, 0),
-                                         (np.float32, 1), (np.float32, 2), (np.float32, 3)])
+                                         (np.float32, 1), (np.float32, 2), (np.float32, 3), (np.float32, 4)])
 def test_apply_every_tile_shape(cuda, pkg, oracle, dtype, shape):
     """Every tile shape of the single-matrix wave kernel gives the oracle's bits (FP32 shapes 2
-    and 3 hold two rows per thread, FP64 shape 2 is a CTA of 27 warps; the row counts leave
-    partial tiles and partial warps)."""
+    and 3 hold two rows per thread, FP32 shape 4 is a CTA of 14 warps, FP64 shape 2 one of 27
+    warps; the row counts leave partial tiles and partial warps)."""
     import ctypes
     lib = pkg.load_library()
     fp64 = int(dtype == np.float64)
@@ -127,7 +127,7 @@ def test_apply_every_tile_shape(cuda, pkg, oracle, dtype, shape):
     assert lib.symeig_apply_tuning(fp64, ctypes.byref(v), 1) == 0
     try:
         rng = np.random.default_rng(99 + shape)
-        for (m, n, k) in [(33, 70, 64), (100, 129, 130), (7, 20, 5), (77, 40, 64), (333, 90, 64)]:
+        for (m, n, k) in [(33, 70, 64), (100, 129, 130), (7, 20, 5), (77, 40, 64), (333, 90, 64), (15100, 50, 64)]:
             g = rotation_grid(pkg, rng, n, k, dtype)
             A = np.asfortranarray((rng.random((m, n)) * 2 - 1).astype(dtype))
             ref = A.copy(order="F")
