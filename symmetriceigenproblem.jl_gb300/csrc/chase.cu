@@ -307,11 +307,27 @@ __device__ __forceinline__ int32_t warp_max(int32_t v)
 // the bracket's midpoint.  The recurrence is rescaled by exact powers of two whenever the
 // exponent of p_i leaves [-600, 600]: over 128 rows of a window whose diagonal lies close to
 // the shift, the unscaled p_i underflows (about 1e-362 in case A), which made every Newton
-// step non-finite and left the shifts at FP32 accuracy.  All 32 lanes of warp 0 call it;
-// lane l finds eigenvalues l, l + 32, ...; sd, se2, sea (FP32) and dd, ee2 (FP64) are
+// step non-finite and left the shifts at FP32 accuracy.  Warp 0 of the controller sets up the
+// window (batch_shifts_setup), then every thread of the CTA solves for its shifts
+// (batch_shifts_solve); sd, se2, sea (FP32) and dd, ee2 (FP64) are
 // kShiftWindow * kMaxBulges-entry shared arrays.
 constexpr int kShiftWindow = 2;
 constexpr int kWinMax = kShiftWindow * kMaxBulges;
+
+// Number of the scaled window's eigenvalues below x, from the FP32 pivots of
+// T - x I = L D L^T (a negative pivot per eigenvalue below x).
+__device__ __forceinline__ int window_count32(const float* sd, const float* se2, int w, float x)
+{
+    constexpr float kPiv = 1e-30f;
+    float q = sd[0] - x;
+    int cnt = q < 0.0f;
+    for (int i = 1; i < w; ++i) {
+        if (fabsf(q) < kPiv) q = -kPiv;
+        q = (sd[i] - x) - se2[i - 1] / q;
+        cnt += q < 0.0f;
+    }
+    return cnt;
+}
 
 // p(x), p'(x) and the number of eigenvalues below x of the scaled window (dd, ee2), in FP64.
 __device__ __forceinline__ void char_poly(const double* __restrict__ dd, const double* __restrict__ ee2, int w,
@@ -346,9 +362,17 @@ __device__ __forceinline__ void char_poly(const double* __restrict__ dd, const d
     below = cnt;
 }
 
-__device__ void batch_shifts(const double* __restrict__ dv, const double* __restrict__ ev, int64_t from,
-                             int64_t to, int nb, double* __restrict__ shifts, float* sd, float* se2,
-                             float* sea, double* dd, double* ee2)
+// What batch_shifts_setup leaves for batch_shifts_solve (shared memory).
+struct ShiftWindow {
+    int32_t w, k0, ex, trivial;
+    float lo, hi;
+};
+
+// Warp 0: load and scale the window into the shared arrays, its Gershgorin interval, and the
+// rank k0 of the first shift.
+__device__ void batch_shifts_setup(const double* __restrict__ dv, const double* __restrict__ ev, int64_t from,
+                                   int64_t to, int nb, ShiftWindow& sw, float* sd, float* se2, float* sea,
+                                   double* dd, double* ee2)
 {
     const int lane = threadIdx.x & 31;
     constexpr int H = kWinMax / 32;
@@ -368,7 +392,10 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
     for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (!(mx > 0.0) || !isfinite(mx)) {
         // a zero block is already diagonal; a non-finite one is left to the sweep
-        for (int j = lane; j < nb; j += 32) shifts[j] = dv[to - nb + j];
+        if (lane == 0) {
+            sw.w = w;
+            sw.trivial = 1;
+        }
         __syncwarp();
         return;
     }
@@ -402,30 +429,37 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
         lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
         hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
     }
-    lo -= 1e-6f;
-    hi += 1e-6f;
-    constexpr float kPiv = 1e-30f;
-    // number of the window's eigenvalues below x (negative pivots of T - x I = L D L^T), FP32
-    auto count32 = [&](float x) {
-        float q = sd[0] - x;
-        int cnt = q < 0.0f;
-        for (int i = 1; i < w; ++i) {
-            if (fabsf(q) < kPiv) q = -kPiv;
-            q = (sd[i] - x) - se2[i - 1] / q;
-            cnt += q < 0.0f;
-        }
-        return cnt;
-    };
     int k0 = 0;
-    if (w > nb) k0 = min(max(count32(sd[w - 1]) - nb / 2, 0), w - nb);
-    for (int j0 = 0; j0 < nb; j0 += 32) {
-        const int j = j0 + lane;       // the shift this lane finds (uniform loop bound)
-        const int k = k0 + min(j, nb - 1);
-        float a = lo, b = hi;
+    if (w > nb) k0 = min(max(window_count32(sd, se2, w, sd[w - 1]) - nb / 2, 0), w - nb);
+    if (lane == 0) {
+        sw.w = w;
+        sw.k0 = k0;
+        sw.ex = ex;
+        sw.trivial = 0;
+        sw.lo = lo - 1e-6f;
+        sw.hi = hi + 1e-6f;
+    }
+    __syncwarp();
+}
+
+// All threads of the CTA (after a barrier that follows the setup): thread j finds shift j,
+// j + blockDim.x, ...  FP32 bisection to a bracket, then the safeguarded FP64 Newton iteration.
+__device__ void batch_shifts_solve(const double* __restrict__ dv, int64_t to, int nb, const ShiftWindow& sw,
+                                   double* __restrict__ shifts, const float* sd, const float* se2,
+                                   const double* dd, const double* ee2)
+{
+    if (sw.trivial) {
+        for (int j = threadIdx.x; j < nb; j += blockDim.x) shifts[j] = dv[to - nb + j];
+        return;
+    }
+    const int w = sw.w;
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+        const int k = sw.k0 + j;
+        float a = sw.lo, b = sw.hi;
         for (int it = 0; it < 40; ++it) {
             const float mid = 0.5f * (a + b);
             if (!(mid > a && mid < b)) break;
-            if (count32(mid) > k) b = mid;
+            if (window_count32(sd, se2, w, mid) > k) b = mid;
             else a = mid;
         }
         // FP64 refinement inside a bracket kept by FP64 Sturm counts
@@ -445,9 +479,8 @@ __device__ void batch_shifts(const double* __restrict__ dv, const double* __rest
             if (!(xn > A && xn < B)) xn = 0.5 * (A + B);
             x = xn;
         }
-        if (j < nb) shifts[j] = ldexp(x, ex);
+        shifts[j] = ldexp(x, sw.ex);
     }
-    __syncwarp();
 }
 
 // The bulges of a batch.  Bulge j (CTA j) runs the two-warp sweep of sweep_nr_2w (same split,
@@ -649,6 +682,7 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
     __shared__ int32_t fail;
     __shared__ float ms_d[kWinMax], ms_e2[kWinMax], ms_ea[kWinMax];
     __shared__ double ms_dd[kWinMax], ms_ee2[kWinMax];
+    __shared__ ShiftWindow swin;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int64_t n = st->n;
@@ -774,7 +808,7 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
                                 nbl = min(nbl, maxiter - iter + 1);
                             }
                             if (nbl >= 2) {
-                                batch_shifts(dv, ev, from, to, (int)nbl, bs->shifts, ms_d, ms_e2, ms_ea, ms_dd, ms_ee2);
+                                batch_shifts_setup(dv, ev, from, to, (int)nbl, swin, ms_d, ms_e2, ms_ea, ms_dd, ms_ee2);
                                 d.bulges = (int32_t)nbl;
                                 d.action = 3;
                             } else {
@@ -799,7 +833,11 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
         __syncthreads();
         const Decision d = dec;
         last = d;
-        if (d.action == 3) break;  // the batch runs in its own launch
+        if (d.action == 3) {
+            // the batch's shifts, one per thread, then the batch runs in its own launch
+            batch_shifts_solve(dv, d.to, d.bulges, swin, bs->shifts, ms_d, ms_e2, ms_dd, ms_ee2);
+            break;
+        }
         if (d.action == 1) {
             // entries the sweep may change: dv[from-1 .. to-1], ev[from-1 .. to-2] (0-based)
             const int64_t q0 = d.from - 1, q1 = d.to - 1;
