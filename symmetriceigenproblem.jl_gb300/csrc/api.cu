@@ -482,7 +482,8 @@ int apply_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T
     CK(h->q.ensure((size_t)m * n * sizeof(T)));
     const size_t cs_bytes = (size_t)(n - 1) * k * 2 * sizeof(T);
     CK(h->cs.ensure(cs_bytes));
-    if (k <= apply_layers_per_pass<T>() && m >= (int64_t)kPipeBlocks * 256 && !h->kernel_timing) {
+    if (k <= apply_layers_per_pass<T>() && m >= (int64_t)kPipeBlocks * 256 && !h->kernel_timing &&
+        apply_host_segmented_supported<T>()) {
         rc = apply_host_pipelined<T>(h, A, lda, m, n, cs, k);
         if (rc) {
             // nothing queued may still read or write the caller's buffer after the return

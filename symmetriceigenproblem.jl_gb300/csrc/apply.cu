@@ -309,7 +309,7 @@ scaled_table_kernel(unsigned char* __restrict__ table, int64_t n_chunks, const T
 // One launch covers chunks [c_begin, c_end) of the pass (all of them unless the pass runs as
 // column segments, see wave_tile); `state` holds the registers carried between segments,
 // segment_state_values * THREADS values per CTA.
-template <typename T, int S, bool SCALED = false, bool INT_MUL = false>
+template <typename T, int S, bool SCALED = false, bool INT_MUL = false, bool SEG = false>
 __global__ void __launch_bounds__(Cfg<T, S>::THREADS, INT_MUL ? Cfg<T, S>::MINB_INT : Cfg<T, S>::MINB)
 wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
                   const unsigned char* __restrict__ table, int32_t n_chunks, int* __restrict__ err,
@@ -322,9 +322,9 @@ wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
     wave::Staging<Sh> st{ring, bar, 0, 0};
     wave::staging_init(st);
     const int64_t row0 = (int64_t)blockIdx.x * Sh::ROWS;
-    T* cta_state = state ? state + (int64_t)blockIdx.x * (wave::segment_state_values<Sh>() * Sh::THREADS) : nullptr;
-    if (!wave::wave_tile<T, Sh, SCALED, INT_MUL>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs, stall,
-                                                 c_begin, c_end, cta_state)) {
+    T* cta_state = (SEG && state) ? state + (int64_t)blockIdx.x * (wave::segment_state_values<Sh>() * Sh::THREADS) : nullptr;
+    if (!wave::wave_tile<T, Sh, SCALED, INT_MUL, SEG>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs, stall,
+                                                      c_begin, c_end, cta_state)) {
         if (threadIdx.x == 0) atomicExch(err, 1);
     }
 }
@@ -463,9 +463,9 @@ cudaError_t prep_pass_shape(const Tsrc* grid, int64_t grid_rows, const int32_t* 
 // The wave kernel over chunks [seg.c_begin, seg.c_end) of one pass, rows [0, m).
 // `int_mul_rows`: the canonical FP64 form takes the integer-pipe products from this many rows
 // of the launch on.
-template <typename T, int S>
-cudaError_t launch_wave_shape(T* Q, int64_t ldq, int64_t m, const ApplyPass& pass, const void* table, int* err,
-                              cudaStream_t stream, const Seg& seg, int64_t int_mul_rows = kIntMulRows)
+template <typename T, int S, bool SEG>
+cudaError_t launch_wave_variant(T* Q, int64_t ldq, int64_t m, const ApplyPass& pass, const void* table, int* err,
+                                cudaStream_t stream, const Seg& seg, int64_t int_mul_rows)
 {
     using Sh = typename Cfg<T, S>::Sh;
     const int64_t n_chunks = Sh::chunks(pass.n_loc);
@@ -475,22 +475,34 @@ cudaError_t launch_wave_shape(T* Q, int64_t ldq, int64_t m, const ApplyPass& pas
     const unsigned char* tb = (const unsigned char*)table;
     if constexpr (sizeof(T) == 8) {
         if (pass.form == 1) {
-            wave_apply_kernel<T, S, true><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
+            wave_apply_kernel<T, S, true, false, SEG><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
                 q, ldq, m, (int32_t)pass.n_loc, tb, (int32_t)n_chunks, err, (T)-0.0, pass.rs, stall,
                 seg.c_begin, seg.c_end, (T*)seg.state);
             return cudaGetLastError();
         }
         if (pass.form == 0 && m >= int_mul_rows) {   // canonical FP64: products on the integer pipes
-            wave_apply_kernel<T, S, false, true><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
+            wave_apply_kernel<T, S, false, true, SEG><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
                 q, ldq, m, (int32_t)pass.n_loc, tb, (int32_t)n_chunks, err, (T)-0.0, pass.rs, stall,
                 seg.c_begin, seg.c_end, (T*)seg.state);
             return cudaGetLastError();
         }
     }
-    wave_apply_kernel<T, S><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
+    wave_apply_kernel<T, S, false, false, SEG><<<(unsigned)blocks, Sh::THREADS, 0, stream>>>(
         q, ldq, m, (int32_t)pass.n_loc, tb, (int32_t)n_chunks, err, (T)-0.0, pass.rs, stall,
         seg.c_begin, seg.c_end, (T*)seg.state);
     return cudaGetLastError();
+}
+
+// The wave kernel over chunks [seg.c_begin, seg.c_end) of one pass, rows [0, m): the whole-pass
+// kernel unless a segment is given.  `int_mul_rows`: the canonical FP64 form takes the
+// integer-pipe products from this many rows of the launch on.
+template <typename T, int S>
+cudaError_t launch_wave_shape(T* Q, int64_t ldq, int64_t m, const ApplyPass& pass, const void* table, int* err,
+                              cudaStream_t stream, const Seg& seg, int64_t int_mul_rows = kIntMulRows)
+{
+    if (seg.state != nullptr)
+        return launch_wave_variant<T, S, true>(Q, ldq, m, pass, table, err, stream, seg, int_mul_rows);
+    return launch_wave_variant<T, S, false>(Q, ldq, m, pass, table, err, stream, seg, int_mul_rows);
 }
 
 template <typename Tsrc, typename T, int S>
@@ -603,19 +615,27 @@ cudaError_t apply_host_segmented(T* dQ, int64_t m, const T* d_cs, const ApplyPas
 {
     if (pass.n_loc < 2 || pass.layers <= 0 || m <= 0) return cudaSuccess;
     if (pass.layers > 64 || pass.c0 != 0 || pass.L0 != 0) return cudaErrorInvalidValue;
+    // segment kernels exist for the default tile shapes only (FP64 0 and its 27-warp form 2,
+    // FP32 2 and its 14-warp form 4); other tunings take the unpipelined path
     const int s = shape_index<T>();
     if constexpr (sizeof(T) == 8) {
         if (s == 2 || (s == 0 && m >= kWideRows))
             return host_segmented_shape<T, 2>(dQ, m, d_cs, pass, table, err, stream, io);
-    }
-    if constexpr (sizeof(T) == 4) {
+        if (s == 0) return host_segmented_shape<T, 0>(dQ, m, d_cs, pass, table, err, stream, io);
+    } else {
         if (s == 4 || (s == 2 && m >= kWideRows)) return host_segmented_shape<T, 4>(dQ, m, d_cs, pass, table, err, stream, io);
         if (s == 2) return host_segmented_shape<T, 2>(dQ, m, d_cs, pass, table, err, stream, io);
-        if (s == 3) return host_segmented_shape<T, 3>(dQ, m, d_cs, pass, table, err, stream, io);
     }
-    if (s == 0) return host_segmented_shape<T, 0>(dQ, m, d_cs, pass, table, err, stream, io);
-    return host_segmented_shape<T, 1>(dQ, m, d_cs, pass, table, err, stream, io);
+    return cudaErrorNotSupported;
 }
+// Whether apply_host_segmented takes the current tile shape of T.
+template <typename T> bool apply_host_segmented_supported()
+{
+    const int s = shape_index<T>();
+    return sizeof(T) == 8 ? (s == 0 || s == 2) : (s == 2 || s == 4);
+}
+template bool apply_host_segmented_supported<double>();
+template bool apply_host_segmented_supported<float>();
 template cudaError_t apply_host_segmented<double>(double*, int64_t, const double*, const ApplyPass&, void*, int*,
                                                   cudaStream_t, const HostStream&);
 template cudaError_t apply_host_segmented<float>(float*, int64_t, const float*, const ApplyPass&, void*, int*,

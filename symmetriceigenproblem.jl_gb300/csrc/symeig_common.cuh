@@ -176,6 +176,7 @@ template <typename T>
 cudaError_t apply_host_segmented(T* dQ, int64_t m, const T* d_cs, const ApplyPass& pass, void* table, int* err,
                                  cudaStream_t stream, const HostStream& io);
 template <typename T> size_t apply_segment_state_bytes(int64_t m);
+template <typename T> bool apply_host_segmented_supported();
 
 // Tile shape of the single-matrix wave kernel per precision (see apply.cu).
 void apply_set_shape(int fp64, int shape);
