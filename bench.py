@@ -690,7 +690,8 @@ def run_solve(args):
 
 def measure_batched(pkg, count=4096, loop_sample=8, check=256, cpu_sample=64, with_cpu=True):
     """Batched eigensolves (qr_algorithm_batched_, one call): `count` tridiagonals with
-    n ~ U{32..1024}, d ~ N(0,1), e ~ U[0.1,1) (seed 3), FP64 Q, against (a) one
+    n ~ U{32..1024}, d ~ N(0,1), e ~ U[0.1,1) (seed 3), FP64 Q (and, as `q32`, the same batch
+    with FP32 Q), against (a) one
     qr_algorithm! call per matrix on the same GPU, timed on a sample of the batch's own
     matrices in the reference's sweep sequence (chase mode 0) and with the multishift chase
     (mode 3), extrapolated by sum n^2 (the apply's work per sweep is n^2 per matrix; the loop
@@ -737,6 +738,29 @@ def measure_batched(pkg, count=4096, loop_sample=8, check=256, cpu_sample=64, wi
                           torch.from_numpy(e[eoff[j]:eoff[j + 1]]).to(dev), td[doff[j]:doff[j + 1]], Qj)
         resid_max, orth_max = max(resid_max, r / (10 * n * eps)), max(orth_max, o / (10 * n * eps))
     del tQ
+    # the same batch with FP32 Q (the FP32-Q variant: FP64 chase, (c,s) rounded to float)
+    td32, te32 = torch.from_numpy(d.copy()).to(dev), torch.from_numpy(e.copy()).to(dev)
+    tQ32 = torch.zeros(int(qoff[-1]), dtype=torch.float32, device=dev)
+    for j, n in enumerate(sizes):
+        tQ32[qoff[j]:qoff[j + 1]].view(n, n).fill_diagonal_(1.0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    conv32, _ = pkg.qr_algorithm_batched_(td32, te32, sizes, tQ32, handle=h)
+    torch.cuda.synchronize()
+    secs32 = time.perf_counter() - t0
+    eps32 = float(np.finfo(np.float32).eps)
+    r32 = o32 = 0.0
+    for j in chk[:16]:
+        n = int(sizes[j])
+        Qj = tQ32[qoff[j]:qoff[j + 1]].view(n, n).T
+        r, o = _tq_errors(torch, torch.from_numpy(d[doff[j]:doff[j + 1]]).to(dev),
+                          torch.from_numpy(e[eoff[j]:eoff[j + 1]]).to(dev), td32[doff[j]:doff[j + 1]], Qj)
+        r32, o32 = max(r32, r / (10 * n * eps32)), max(o32, o / (10 * n * eps32))
+    q32 = {"value": round(count / secs32, 2), "unit": "solves/s", "seconds": round(secs32, 3),
+           "all_converged": bool(conv32.all()),
+           "same_eigenvalues_as_f64": bool(torch.equal(td32, torch.from_numpy(lam_all).to(dev))),
+           "resid_over_10n_eps32_max": r32, "orth_over_10n_eps32_max": o32, "vectors_checked": 16}
+    del tQ32, td32, te32
     # (a) one call per matrix, on the batch's own matrices
     sample = rng.choice(count, min(loop_sample, count), replace=False)
     w_all = float((sizes.astype(np.float64) ** 2).sum())
@@ -761,7 +785,7 @@ def measure_batched(pkg, count=4096, loop_sample=8, check=256, cpu_sample=64, wi
     best_loop = min(loop["mode0"]["extrapolated_seconds"], loop["mode3"]["extrapolated_seconds"])
     out = {"value": round(count / secs, 2), "unit": "solves/s", "count": count, "seconds": round(secs, 3),
            "all_converged": bool(conv.all()), "iterations": int(iters.sum()), "rounds": st["flushes"],
-           "tuning": tuning[0], "loop": loop,
+           "tuning": tuning[0], "autotune_ms": tuning[1], "q32": q32, "loop": loop,
            "speedup_vs_loop_mode0": round(loop["mode0"]["extrapolated_seconds"] / secs, 1),
            "speedup_vs_best_loop": round(best_loop / secs, 1),
            "errors": {"eig_err_over_10n_eps_normT_max": eig_ratio, "eig_checked": int(len(chk)),

@@ -98,6 +98,11 @@ int symeig_set_chase_mode(symeig_handle h, int32_t mode);
  * [1, 64] (default 4).  No reference counterpart. */
 int symeig_set_multishift(symeig_handle h, int32_t max_bulges, int32_t rows_per_bulge,
                           int32_t release_every);
+/* Fewest bulges of a chase-mode-3 batch: a block with room for fewer (len / rows_per_bulge,
+ * capped by max_bulges and the layer room) takes one sweep with the reference's Wilkinson
+ * shift instead, which avoids a batch's launches and shift solve on short blocks.
+ * min_bulges in [2, 128]; default 2.  No reference counterpart. */
+int symeig_set_multishift_min(symeig_handle h, int32_t min_bulges);
 /* Arithmetic form of the FP64 bulk apply (symeig_apply_givens_f64*, and the qr driver's
  * apply with FP64 Q).  0 (default): every rotation as the reference's rmul!, two products and
  * two FMAs per rotation and row; from 3072 rows of Q on, the two products are computed on the
@@ -195,11 +200,28 @@ int symeig_qr_batched_f64(symeig_handle h, int64_t count, const int64_t* n, doub
 int symeig_qr_batched_f64_dev(symeig_handle h, int64_t count, const int64_t* n, double* d,
                               double* e, double* Q, int32_t max_layers, double tol,
                               int64_t maxiter_factor, int32_t* converged, int64_t* iters);
-/* Autotuner of the batched apply: times each candidate tile shape (0: 16 rows x 8 layer
- * groups of 8; 1: 32 rows x 4 groups of 16 -- both 64 layers per pass) on a synthetic batch
- * of each size class (n <= split, n > split) and keeps the faster one per class, process-wide.
- * ms (may be NULL) receives 4 timings [class][shape].  No reference counterpart. */
+/* The same batched solve with an FP32 Q (the FP32-Q variant of qr_algorithm!: the chase and
+ * the rotations stay FP64, each (c,s) is rounded to float and applied to the FP32 Q).  Same
+ * packed layout, Q of sum n_i^2 floats.  No reference counterpart. */
+int symeig_qr_batched_f64_q32(symeig_handle h, int64_t count, const int64_t* n, double* d, double* e,
+                              float* Q, int32_t max_layers, double tol, int64_t maxiter_factor,
+                              int32_t* converged, int64_t* iters);
+int symeig_qr_batched_f64_q32_dev(symeig_handle h, int64_t count, const int64_t* n, double* d,
+                                  double* e, float* Q, int32_t max_layers, double tol,
+                                  int64_t maxiter_factor, int32_t* converged, int64_t* iters);
+/* Autotuner of the batched apply: for each precision of Q and each size class (n <= split,
+ * n > split) it times every candidate tile on a synthetic batch of that class (one 128-layer
+ * flush of every matrix; orders spread over the class: 2048 matrices of n = 32 .. split, 512
+ * of n = split + 1 .. 4 split) and keeps the fastest per (class, precision), process-wide.  Tiles: 0 = 16 rows x 8
+ * lane groups of 8 layers, 1 = 32 rows x 4 groups of 16 layers (both 64 layers per pass),
+ * 2 = 8 rows x 16 groups of 8 layers (128 layers per pass: a whole flush in one pass).  ms
+ * (may be NULL) receives 12 timings, ms[(dtype * 2 + class) * 3 + tile] with dtype 0 = FP64 Q,
+ * 1 = FP32 Q.  No reference counterpart. */
 int symeig_batched_autotune(symeig_handle h, double* ms);
+/* The same with the orders of the batch to be solved (count entries of n, host array): each
+ * class is timed on those of its orders (thinned evenly to 1.5 GiB of FP64 Q), a class with
+ * none on the spread above.  No reference counterpart. */
+int symeig_batched_autotune_sizes(symeig_handle h, int64_t count, const int64_t* n, double* ms);
 /* Read (set = 0) or write (set != 0) the tile shape of the single-matrix wave kernel for FP64
  * (fp64 != 0) or FP32: 0 = 8 lane groups of 8 layers (4 rows per warp), 1 = 4 groups of 16
  * layers (8 rows per warp); FP32 only: 2 = shape 1 and 3 = shape 0 with two rows per thread,
@@ -209,7 +231,12 @@ int symeig_batched_autotune(symeig_handle h, double* ms);
  * precision lacks.
  * Process-wide.  No reference counterpart. */
 int symeig_apply_tuning(int32_t fp64, int32_t* shape, int32_t set);
-/* Read (set = 0) or write (set != 0) the batched tuning: class split and shape per class. */
+/* Read (set = 0) or write (set != 0) the batched tuning of FP64 Q (fp64 != 0) or FP32 Q: the
+ * class split and the tile (0..2, as for the autotuner) per class.  SYMEIG_ERR_SIZE for a split
+ * below 1 or a tile out of range.  Defaults: split 256, tile 0 for both classes. */
+int symeig_batched_tuning_dtype(int32_t fp64, int64_t* split, int32_t* shape_small, int32_t* shape_large,
+                                int32_t set);
+/* symeig_batched_tuning_dtype for FP64 Q. */
 int symeig_batched_tuning(int64_t* split, int32_t* shape_small, int32_t* shape_large, int32_t set);
 
 /* ---- adjoint (reverse-mode derivative) of the eigensolve ------------------------------------ *

@@ -76,7 +76,7 @@ def _bind(L):
                                      ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)]
         L.oracle_qr_form.restype = ctypes.c_int
         L.oracle_qr_multishift.argtypes = [c_vp, c_vp, c_i64, c_vp, c_i64, c_i64, c_i32, c_dbl, c_i64, c_i32,
-                                           c_i32, c_i32, c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(c_i64),
+                                           c_i32, c_i32, c_i32, c_i32, ctypes.POINTER(c_i32), ctypes.POINTER(c_i64),
                                            ctypes.POINTER(c_i64), ctypes.POINTER(c_i64), ctypes.POINTER(c_i64)]
         L.oracle_qr_multishift.restype = ctypes.c_int
         L.oracle_apply_scaled_f64.argtypes = [c_vp, c_i64, c_i64, c_i64, c_vp, c_i64]
@@ -244,13 +244,18 @@ def qr_algorithm(d: np.ndarray, e: np.ndarray, Q: np.ndarray | None, max_layers:
     return bool(conv.value), it.value, fl.value, rot.value
 
 
+# The device's default fewest bulges of a multishift batch (symeig_set_multishift_min).
+MS_MIN_DEFAULT = 2
+
+
 def qr_multishift(d: np.ndarray, e: np.ndarray, Q: np.ndarray | None, max_layers: int = 128,
                   tol: float | None = None, maxiter: int | None = None, exact_order: bool = True,
-                  ms_bulges: int = 64, ms_rows: int = 16, ms_window: int = 2):
+                  ms_bulges: int = 64, ms_rows: int = 16, ms_window: int = 2, ms_min: int = MS_MIN_DEFAULT):
     """The device's multishift chase (chase mode 3) restated: batches of up to ms_bulges
     sweeps whose shifts are eigenvalues of the block's trailing window of ms_window times the
     batch's size (ranked about the bottom entry), run in sequence with the reference's
-    rotations (oracle_qr_multishift).  Not the reference's algorithm; its results are judged
+    rotations (oracle_qr_multishift); a block with room for fewer than ms_min bulges takes a
+    single sweep with the reference's shift.  Not the reference's algorithm; its results are judged
     by the reference's error bounds.  FP64 Q or None.
     Returns (converged, iter, flushes, rotations, batches)."""
     n = d.shape[0]
@@ -266,7 +271,8 @@ def qr_multishift(d: np.ndarray, e: np.ndarray, Q: np.ndarray | None, max_layers
         m, ld, qp = 0, 1, None
     ebuf = e if e.size else np.zeros(1)
     rc = lib().oracle_qr_multishift(_ptr(d), _ptr(ebuf), n, qp, ld, m, max_layers, tol, maxiter,
-                                    int(exact_order), int(ms_bulges), int(ms_rows), int(ms_window), ctypes.byref(conv),
+                                    int(exact_order), int(ms_bulges), int(ms_rows), int(ms_window), int(ms_min),
+                                    ctypes.byref(conv),
                                     ctypes.byref(it), ctypes.byref(fl), ctypes.byref(rot), ctypes.byref(bat))
     if rc != 0:
         raise RuntimeError(f"oracle_qr_multishift failed with status {rc}")

@@ -507,6 +507,7 @@ typedef struct {
     int32_t ms_bulges;          /* multishift batches: bulge cap (0: single shifts only) */
     int32_t ms_rows;            /* multishift batches: block rows per bulge */
     int32_t ms_window;          /* multishift batches: shift window, in multiples of the bulges */
+    int32_t ms_min;             /* multishift batches: fewest bulges of a batch (else a single sweep) */
     int64_t batches;            /* multishift batches run */
 } oracle_qr_state;
 
@@ -634,6 +635,7 @@ int oracle_qr_flush(oracle_qr_state* st, double* dv, double* ev, double* givens,
                     if (nbl > st->ms_bulges) nbl = st->ms_bulges;
                     if (nbl > cap) nbl = cap;
                     if (nbl > st->maxiter - st->iter + 1) nbl = st->maxiter - st->iter + 1;
+                    if (nbl < st->ms_min) nbl = 1;
                 }
                 did_a_thing = 1;
                 if (nbl >= 2) {
@@ -689,8 +691,8 @@ int oracle_qr(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, 
 static int oracle_qr_driver(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
                             int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
                             int32_t apply_form, int32_t ms_bulges, int32_t ms_rows, int32_t ms_window,
-                            int32_t* converged, int64_t* iter, int64_t* flushes, int64_t* rotations,
-                            int64_t* batches);
+                            int32_t ms_min, int32_t* converged, int64_t* iter, int64_t* flushes,
+                            int64_t* rotations, int64_t* batches);
 
 int oracle_qr_form(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
                    int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
@@ -698,31 +700,34 @@ int oracle_qr_form(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_
                    int64_t* rotations)
 {
     return oracle_qr_driver(d, e, n, Q, ldq, m, q_is_f32, max_layers, tol, maxiter, exact_order,
-                            apply_form, 0, 16, 1, converged, iter, flushes, rotations, NULL);
+                            apply_form, 0, 16, 1, 2, converged, iter, flushes, rotations, NULL);
 }
 
 /* The device's multishift chase (chase mode 3; not the reference's algorithm, which is
  * oracle_qr) restated: where a block has room, a batch of up to ms_bulges sweeps
- * (min(ms_bulges, len / ms_rows), the layer room and maxiter decide) with the eigenvalues of
+ * (min(ms_bulges, len / ms_rows), the layer room and maxiter decide; fewer than ms_min make a
+ * single sweep with the reference's shift instead) with the eigenvalues of
  * a trailing window of ms_window times the batch's size as shifts (oracle_trailing_eigenvalues),
  * run as sweeps in sequence with the reference's rotations; every other decision, the apply
  * and the placement as in oracle_qr.  FP64 Q, canonical apply.  *batches receives the number
  * of batches. */
 int oracle_qr_multishift(double* d, double* e, int64_t n, double* Q, int64_t ldq, int64_t m,
                          int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
-                         int32_t ms_bulges, int32_t ms_rows, int32_t ms_window, int32_t* converged,
-                         int64_t* iter, int64_t* flushes, int64_t* rotations, int64_t* batches)
+                         int32_t ms_bulges, int32_t ms_rows, int32_t ms_window, int32_t ms_min,
+                         int32_t* converged, int64_t* iter, int64_t* flushes, int64_t* rotations,
+                         int64_t* batches)
 {
     if (ms_bulges < 2 || ms_bulges > 128 || ms_rows < 4 || ms_window < 1 || ms_window > 4) return 1;
+    if (ms_min < 2 || ms_min > ms_bulges) return 1;
     return oracle_qr_driver(d, e, n, Q, ldq, m, 0, max_layers, tol, maxiter, exact_order, 0, ms_bulges,
-                            ms_rows, ms_window, converged, iter, flushes, rotations, batches);
+                            ms_rows, ms_window, ms_min, converged, iter, flushes, rotations, batches);
 }
 
 static int oracle_qr_driver(double* d, double* e, int64_t n, void* Q, int64_t ldq, int64_t m, int q_is_f32,
                             int32_t max_layers, double tol, int64_t maxiter, int32_t exact_order,
                             int32_t apply_form, int32_t ms_bulges, int32_t ms_rows, int32_t ms_window,
-                            int32_t* converged, int64_t* iter, int64_t* flushes, int64_t* rotations,
-                            int64_t* batches)
+                            int32_t ms_min, int32_t* converged, int64_t* iter, int64_t* flushes,
+                            int64_t* rotations, int64_t* batches)
 {
     if (apply_form != 0 && q_is_f32) return 1;
     if (n < 1 || max_layers < 1 || (Q && ldq < m)) return 1;
@@ -731,6 +736,7 @@ static int oracle_qr_driver(double* d, double* e, int64_t n, void* Q, int64_t ld
     st.ms_bulges = ms_bulges;
     st.ms_rows = ms_rows;
     st.ms_window = ms_window;
+    st.ms_min = ms_min;
     int64_t nr = n > 1 ? n - 1 : 1;
     int64_t GL = st.grid_layers;
     double* givens = (double*)malloc(sizeof(double) * 2 * nr * GL);

@@ -12,6 +12,7 @@ from .api import (  # noqa: F401
     bulk_wave_order_2x2_rmul_parallel_,
     eig_adjoint,
     batched_autotune,
+    batched_tuning,
     qr_algorithm_batched_,
     eigen_decomp_,
     get_rotation,

@@ -34,6 +34,7 @@ SIGNATURES = {
     "symeig_set_exact_order": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_chase_mode": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_multishift": (ctypes.c_int, [c_vp, c_i32, c_i32, c_i32]),
+    "symeig_set_multishift_min": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_apply_form": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_set_test_stall": (ctypes.c_int, [c_vp, c_i32]),
     "symeig_get_rotation_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp]),
@@ -68,7 +69,11 @@ SIGNATURES = {
     "symeig_qr_batched_f64": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_dbl, c_i64, c_vp, c_vp]),
     "symeig_qr_batched_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_dbl, c_i64, c_vp, c_vp]),
     "symeig_batched_autotune": (ctypes.c_int, [c_vp, c_vp]),
+    "symeig_batched_autotune_sizes": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp]),
     "symeig_batched_tuning": (ctypes.c_int, [P_i64, P_i32, P_i32, c_i32]),
+    "symeig_batched_tuning_dtype": (ctypes.c_int, [c_i32, P_i64, P_i32, P_i32, c_i32]),
+    "symeig_qr_batched_f64_q32": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_dbl, c_i64, c_vp, c_vp]),
+    "symeig_qr_batched_f64_q32_dev": (ctypes.c_int, [c_vp, c_i64, c_vp, c_vp, c_vp, c_vp, c_i32, c_dbl, c_i64, c_vp, c_vp]),
     "symeig_apply_tuning": (ctypes.c_int, [c_i32, P_i32, c_i32]),
     "symeig_eig_adjoint_f64": (ctypes.c_int, [c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
     "symeig_eig_adjoint_f64_dev": (ctypes.c_int, [c_vp, c_i64, c_i64, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp]),
@@ -170,6 +175,10 @@ class Handle:
         """Batch shape of chase mode 3 (symeig_set_multishift)."""
         check("symeig_set_multishift", self._lib.symeig_set_multishift(
             self.ptr, int(max_bulges), int(rows_per_bulge), int(release_every)))
+
+    def set_multishift_min(self, min_bulges: int = 2):
+        """Fewest bulges of a chase-mode-3 batch (symeig_set_multishift_min)."""
+        check("symeig_set_multishift_min", self._lib.symeig_set_multishift_min(self.ptr, int(min_bulges)))
 
     def set_chase_mode(self, mode):
         """0: Newton-form two-warp chase (default); 1: reference form; 2: Newton form with

@@ -22,7 +22,7 @@ from dataclasses import dataclass
 
 import numpy as np
 
-from ._lib import default_handle, Handle, c_i32, c_i64
+from ._lib import check, default_handle, Handle, c_i32, c_i64, load as load_library
 
 try:  # torch is optional for host-buffer use
     import torch
@@ -281,22 +281,27 @@ def qr_algorithm_batched_(d, e, n, Q=None, max_layers: int = 128, tol: float | N
     d, e, Q are packed: matrix i has order n[i], its diagonal/off-diagonal follow the previous
     matrices' in d (sum n) and e (sum n-1), and its Q (n_i x n_i column-major) follows the
     previous ones in Q (sum n^2, flat).  All three are numpy arrays (host) or CUDA torch
-    tensors (device); Q may be None (eigenvalues only).  Returns (converged, iters) numpy
-    arrays of length count."""
+    tensors (device); Q may be None (eigenvalues only).  d and e are float64; Q is float64 or
+    float32 (the FP32-Q variant: the chase stays FP64 and each (c,s) is rounded to float).
+    Returns (converged, iters) numpy arrays of length count."""
     n = np.ascontiguousarray(np.asarray(n, dtype=np.int64))
     count = int(n.shape[0])
     conv = np.zeros(count, dtype=np.int32)
     iters = np.zeros(count, dtype=np.int64)
     tol = EPS64 if tol is None else float(tol)
     dev = _is_torch(d)
-    arrays = (d, e) + ((Q,) if Q is not None else ())
-    for a in arrays:
+    for a, what in ((d, "d"), (e, "e")) + (((Q, "Q"),) if Q is not None else ()):
         if dev:
-            if not (_is_torch(a) and a.is_cuda and a.dtype == torch.float64 and a.is_contiguous()):
-                raise TypeError("d, e, Q must all be contiguous CUDA float64 tensors")
+            ok = _is_torch(a) and a.is_cuda and a.is_contiguous() and (
+                a.dtype == torch.float64 or (what == "Q" and a.dtype == torch.float32))
+            if not ok:
+                raise TypeError("d, e must be contiguous CUDA float64 tensors, Q float64 or float32")
         else:
-            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous and a.flags.writeable):
-                raise TypeError("d, e, Q must all be writeable contiguous float64 numpy arrays")
+            ok = isinstance(a, np.ndarray) and a.flags.c_contiguous and a.flags.writeable and (
+                a.dtype == np.float64 or (what == "Q" and a.dtype == np.float32))
+            if not ok:
+                raise TypeError("d, e must be writeable contiguous float64 numpy arrays, Q float64 or float32")
+    q32 = Q is not None and (Q.dtype == torch.float32 if dev else Q.dtype == np.float32)
     if int(d.shape[0]) != int(n.sum()) or int(e.shape[0]) != int((n - 1).sum()):
         raise ValueError("packed d / e sizes do not match n")
     if Q is not None and int(Q.numel() if dev else Q.size) != int((n * n).sum()):
@@ -307,25 +312,57 @@ def qr_algorithm_batched_(d, e, n, Q=None, max_layers: int = 128, tol: float | N
             ctypes.c_void_p(ptr(e) if int(e.shape[0]) else None),
             ctypes.c_void_p(ptr(Q) if Q is not None else None), int(max_layers), tol,
             int(maxiter_factor), ctypes.c_void_p(conv.ctypes.data), ctypes.c_void_p(iters.ctypes.data))
+    fn = "symeig_qr_batched_f64_q32" if q32 else "symeig_qr_batched_f64"
     if dev:
         with h.on_stream(torch.cuda.current_stream(d.device).cuda_stream):
-            h.call("symeig_qr_batched_f64_dev", *args)
+            h.call(fn + "_dev", *args)
     else:
         if int(e.shape[0]) == 0:
             ebuf = np.zeros(1)
             args = args[:3] + (ctypes.c_void_p(ebuf.ctypes.data),) + args[4:]
-        h.call("symeig_qr_batched_f64", *args)
+        h.call(fn, *args)
     return conv.astype(bool), iters
 
 
-def batched_autotune(handle: Handle | None = None):
-    """Run the batched-apply autotuner; returns ({class: shape}, timings ms [class][shape])."""
+BATCHED_TILES = 3   # 0: 16 rows x 64 layers, 1: 32 rows x 64 layers, 2: 8 rows x 128 layers
+
+
+def batched_tuning(fp64: bool = True, split: int | None = None, shape_small: int | None = None,
+                   shape_large: int | None = None, handle: Handle | None = None):
+    """Read, or with any argument given write, the batched tuning of FP64 (fp64=True) or FP32 Q:
+    {"split", "shape_small", "shape_large"} (tiles 0..2).  Process-wide; needs no device."""
+    lib = handle._lib if handle is not None else load_library()
+    sp, s0, s1 = c_i64(), c_i32(), c_i32()
+    check("symeig_batched_tuning_dtype",
+          lib.symeig_batched_tuning_dtype(int(fp64), ctypes.byref(sp), ctypes.byref(s0), ctypes.byref(s1), 0))
+    if split is not None or shape_small is not None or shape_large is not None:
+        sp = c_i64(sp.value if split is None else int(split))
+        s0 = c_i32(s0.value if shape_small is None else int(shape_small))
+        s1 = c_i32(s1.value if shape_large is None else int(shape_large))
+        check("symeig_batched_tuning_dtype",
+              lib.symeig_batched_tuning_dtype(int(fp64), ctypes.byref(sp), ctypes.byref(s0), ctypes.byref(s1), 1))
+    return {"split": sp.value, "shape_small": s0.value, "shape_large": s1.value}
+
+
+def batched_autotune(sizes=None, handle: Handle | None = None):
+    """Run the batched-apply autotuner over the tiles (rows per tile and layers per pass) for FP64
+    and FP32 Q, on matrices of the orders `sizes` (those of the batch to be solved; None: a
+    spread of orders over each size class).  Returns ({"f64": tuning, "f32": tuning},
+    {"f64": ms, "f32": ms}) where ms[class][tile] is the time of one 128-layer flush of every
+    matrix of that class."""
     h = handle or default_handle(0)
-    ms = (ctypes.c_double * 4)()
-    h.call("symeig_batched_autotune", ms)
-    split, s0, s1 = c_i64(), c_i32(), c_i32()
-    h._lib.symeig_batched_tuning(ctypes.byref(split), ctypes.byref(s0), ctypes.byref(s1), 0)
-    return {"split": split.value, "shape_small": s0.value, "shape_large": s1.value}, [list(ms[0:2]), list(ms[2:4])]
+    nt = BATCHED_TILES
+    ms = (ctypes.c_double * (4 * nt))()
+    if sizes is None:
+        h.call("symeig_batched_autotune", ms)
+    else:
+        nn = np.ascontiguousarray(np.asarray(sizes, dtype=np.int64))
+        h.call("symeig_batched_autotune_sizes", int(nn.shape[0]), ctypes.c_void_p(nn.ctypes.data), ms)
+    tun, times = {}, {}
+    for dt, name in ((0, "f64"), (1, "f32")):
+        tun[name] = batched_tuning(fp64=(dt == 0), handle=h)
+        times[name] = [list(ms[(dt * 2 + c) * nt:(dt * 2 + c + 1) * nt]) for c in range(2)]
+    return tun, times
 
 
 def _dense_square(A, what="A"):

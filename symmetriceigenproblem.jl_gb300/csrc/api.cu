@@ -74,6 +74,7 @@ struct symeig_context {
     int32_t ms_bulges = kDefaultBulges;      // symeig_set_multishift
     int32_t ms_rows = kDefaultRowsPerBulge;
     int32_t ms_prog_every = kDefaultProgEvery;
+    int32_t ms_min_bulges = kDefaultMinBulges;  // symeig_set_multishift_min
     ChaseState* h_state = nullptr;  // pinned
     std::vector<cudaEvent_t> timing;  // pool of timing events
     symeig_stats stats{};
@@ -260,6 +261,7 @@ int qr_dev(symeig_handle h, double* d, double* e, int64_t n, T* Q, int64_t ldq, 
     init.ms_bulges = h->ms_bulges;
     init.ms_rows = h->ms_rows;
     init.ms_prog_mask = h->ms_prog_every - 1;
+    init.ms_min_bulges = h->ms_min_bulges;
     init.test_stall = h->test_stall;
     ChaseState* dstate = (ChaseState*)h->state.ptr;
 
@@ -590,6 +592,74 @@ int dense_args(symeig_handle h, int64_t n, const void* A, int64_t lda)
 
 }  // namespace
 
+namespace {
+
+// Batched solve with d, e and Q on the device; Q is FP64 or FP32.
+template <typename T>
+int qr_batched_dev_entry(symeig_handle h, int64_t count, const int64_t* n, double* d, double* e, T* Q,
+                         int32_t max_layers, double tol, int64_t maxiter_factor, int32_t* converged,
+                         int64_t* iters)
+{
+    NvtxRange nv("symeig qr batched");
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (count < 0) return SYMEIG_ERR_SIZE;
+    if (count > 0 && (!n || !d || !e)) return SYMEIG_ERR_NULL;
+    if (max_layers < 1) return SYMEIG_ERR_LAYERS;
+    begin_call(h);
+    auto t0 = std::chrono::steady_clock::now();
+    // The rounds are captured as a CUDA graph, which needs a capturable stream (not the legacy
+    // default stream): run on the handle's own stream, ordered after the caller's stream.
+    CK(cudaEventRecord(h->ev_main, h->stream));
+    CK(cudaStreamWaitEvent(h->own_stream, h->ev_main, 0));
+    rc = qr_batched_dev<T>(h->device, h->own_stream, count, n, d, e, Q, max_layers, tol, maxiter_factor,
+                           h->exact_order, converged, iters, &h->stats.flushes, nullptr);
+    for (int64_t i = 0; i < count && iters; ++i) h->stats.iterations += iters[i];
+    h->stats.total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return rc;
+}
+
+// Batched solve with host d, e and Q: copies in, the device solve, copies out.
+template <typename T>
+int qr_batched_host_entry(symeig_handle h, int64_t count, const int64_t* n, double* d, double* e, T* Q,
+                          int32_t max_layers, double tol, int64_t maxiter_factor, int32_t* converged,
+                          int64_t* iters)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (count < 0) return SYMEIG_ERR_SIZE;
+    if (count == 0) return SYMEIG_OK;
+    if (!n || !d || !e) return SYMEIG_ERR_NULL;
+    int64_t nd = 0, ne = 0, nq = 0;
+    for (int64_t i = 0; i < count; ++i) {
+        if (n[i] < 1) return SYMEIG_ERR_SIZE;
+        nd += n[i];
+        ne += n[i] - 1;
+        nq += n[i] * n[i];
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = h->stream;
+    CK(h->d.ensure(nd * sizeof(double)));
+    CK(h->e.ensure(std::max<int64_t>(ne, 1) * sizeof(double)));
+    if (Q) CK(h->q.ensure(nq * sizeof(T)));
+    CK(cudaMemcpyAsync(h->d.ptr, d, nd * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (ne) CK(cudaMemcpyAsync(h->e.ptr, e, ne * sizeof(double), cudaMemcpyHostToDevice, s));
+    if (Q) CK(cudaMemcpyAsync(h->q.ptr, Q, nq * sizeof(T), cudaMemcpyHostToDevice, s));
+    rc = qr_batched_dev_entry<T>(h, count, n, (double*)h->d.ptr, (double*)h->e.ptr, Q ? (T*)h->q.ptr : nullptr,
+                                 max_layers, tol, maxiter_factor, converged, iters);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(d, h->d.ptr, nd * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (ne) CK(cudaMemcpyAsync(e, h->e.ptr, ne * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (Q) CK(cudaMemcpyAsync(Q, h->q.ptr, nq * sizeof(T), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    h->stats.total_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+    return SYMEIG_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int symeig_apply_givens_left_f64(symeig_handle h, double* A, int64_t lda, int64_t m, int64_t n,
@@ -731,6 +801,14 @@ int symeig_set_multishift(symeig_handle h, int32_t max_bulges, int32_t rows_per_
     return SYMEIG_OK;
 }
 
+int symeig_set_multishift_min(symeig_handle h, int32_t min_bulges)
+{
+    if (!h) return SYMEIG_ERR_HANDLE;
+    if (min_bulges < 2 || min_bulges > kMaxBulges) return SYMEIG_ERR_SIZE;
+    h->ms_min_bulges = min_bulges;
+    return SYMEIG_OK;
+}
+
 int symeig_set_apply_form(symeig_handle h, int32_t form)
 {
     if (!h) return SYMEIG_ERR_HANDLE;
@@ -856,65 +934,33 @@ int symeig_apply_givens_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t 
     return apply_dev<float>(h, A, lda, m, n, cs, k);
 }
 
+
 int symeig_qr_batched_f64_dev(symeig_handle h, int64_t count, const int64_t* n, double* d,
                               double* e, double* Q, int32_t max_layers, double tol,
                               int64_t maxiter_factor, int32_t* converged, int64_t* iters)
 {
-    NvtxRange nv("symeig qr batched");
-    int rc = check_handle(h);
-    if (rc) return rc;
-    if (count < 0) return SYMEIG_ERR_SIZE;
-    if (count > 0 && (!n || !d || !e)) return SYMEIG_ERR_NULL;
-    if (max_layers < 1) return SYMEIG_ERR_LAYERS;
-    begin_call(h);
-    auto t0 = std::chrono::steady_clock::now();
-    // The rounds are captured as a CUDA graph, which needs a capturable stream (not the legacy
-    // default stream): run on the handle's own stream, ordered after the caller's stream.
-    CK(cudaEventRecord(h->ev_main, h->stream));
-    CK(cudaStreamWaitEvent(h->own_stream, h->ev_main, 0));
-    rc = qr_batched_dev(h->device, h->own_stream, count, n, d, e, Q, max_layers, tol, maxiter_factor,
-                        h->exact_order, converged, iters, &h->stats.flushes, nullptr);
-    for (int64_t i = 0; i < count && iters; ++i) h->stats.iterations += iters[i];
-    h->stats.total_ms =
-        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    return rc;
+    return qr_batched_dev_entry<double>(h, count, n, d, e, Q, max_layers, tol, maxiter_factor, converged, iters);
 }
 
 int symeig_qr_batched_f64(symeig_handle h, int64_t count, const int64_t* n, double* d, double* e,
                           double* Q, int32_t max_layers, double tol, int64_t maxiter_factor,
                           int32_t* converged, int64_t* iters)
 {
-    int rc = check_handle(h);
-    if (rc) return rc;
-    if (count < 0) return SYMEIG_ERR_SIZE;
-    if (count == 0) return SYMEIG_OK;
-    if (!n || !d || !e) return SYMEIG_ERR_NULL;
-    int64_t nd = 0, ne = 0, nq = 0;
-    for (int64_t i = 0; i < count; ++i) {
-        if (n[i] < 1) return SYMEIG_ERR_SIZE;
-        nd += n[i];
-        ne += n[i] - 1;
-        nq += n[i] * n[i];
-    }
-    auto t0 = std::chrono::steady_clock::now();
-    cudaStream_t s = h->stream;
-    CK(h->d.ensure(nd * sizeof(double)));
-    CK(h->e.ensure(std::max<int64_t>(ne, 1) * sizeof(double)));
-    if (Q) CK(h->q.ensure(nq * sizeof(double)));
-    CK(cudaMemcpyAsync(h->d.ptr, d, nd * sizeof(double), cudaMemcpyHostToDevice, s));
-    if (ne) CK(cudaMemcpyAsync(h->e.ptr, e, ne * sizeof(double), cudaMemcpyHostToDevice, s));
-    if (Q) CK(cudaMemcpyAsync(h->q.ptr, Q, nq * sizeof(double), cudaMemcpyHostToDevice, s));
-    rc = symeig_qr_batched_f64_dev(h, count, n, (double*)h->d.ptr, (double*)h->e.ptr,
-                                   Q ? (double*)h->q.ptr : nullptr, max_layers, tol,
-                                   maxiter_factor, converged, iters);
-    if (rc) return rc;
-    CK(cudaMemcpyAsync(d, h->d.ptr, nd * sizeof(double), cudaMemcpyDeviceToHost, s));
-    if (ne) CK(cudaMemcpyAsync(e, h->e.ptr, ne * sizeof(double), cudaMemcpyDeviceToHost, s));
-    if (Q) CK(cudaMemcpyAsync(Q, h->q.ptr, nq * sizeof(double), cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    h->stats.total_ms =
-        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    return SYMEIG_OK;
+    return qr_batched_host_entry<double>(h, count, n, d, e, Q, max_layers, tol, maxiter_factor, converged, iters);
+}
+
+int symeig_qr_batched_f64_q32_dev(symeig_handle h, int64_t count, const int64_t* n, double* d,
+                                  double* e, float* Q, int32_t max_layers, double tol,
+                                  int64_t maxiter_factor, int32_t* converged, int64_t* iters)
+{
+    return qr_batched_dev_entry<float>(h, count, n, d, e, Q, max_layers, tol, maxiter_factor, converged, iters);
+}
+
+int symeig_qr_batched_f64_q32(symeig_handle h, int64_t count, const int64_t* n, double* d, double* e,
+                              float* Q, int32_t max_layers, double tol, int64_t maxiter_factor,
+                              int32_t* converged, int64_t* iters)
+{
+    return qr_batched_host_entry<float>(h, count, n, d, e, Q, max_layers, tol, maxiter_factor, converged, iters);
 }
 
 int symeig_apply_tuning(int32_t fp64, int32_t* shape, int32_t set)
@@ -933,20 +979,38 @@ int symeig_batched_autotune(symeig_handle h, double* ms)
 {
     int rc = check_handle(h);
     if (rc) return rc;
-    return batched_autotune(h->device, h->stream, ms);
+    return batched_autotune(h->device, h->stream, 0, nullptr, ms);
+}
+
+int symeig_batched_autotune_sizes(symeig_handle h, int64_t count, const int64_t* n, double* ms)
+{
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (count < 0) return SYMEIG_ERR_SIZE;
+    if (count > 0 && !n) return SYMEIG_ERR_NULL;
+    for (int64_t i = 0; i < count; ++i)
+        if (n[i] < 1 || n[i] > (1 << 20)) return SYMEIG_ERR_SIZE;
+    return batched_autotune(h->device, h->stream, count, n, ms);
+}
+
+int symeig_batched_tuning_dtype(int32_t fp64, int64_t* split, int32_t* shape_small, int32_t* shape_large,
+                                int32_t set)
+{
+    if (!split || !shape_small || !shape_large) return SYMEIG_ERR_NULL;
+    if (set) {
+        const int nt = batched_num_tiles();
+        if (*split < 1 || *shape_small < 0 || *shape_small >= nt || *shape_large < 0 || *shape_large >= nt)
+            return SYMEIG_ERR_SIZE;
+        batched_set_tuning(fp64, *split, *shape_small, *shape_large);
+    } else {
+        batched_get_tuning(fp64, split, shape_small, shape_large);
+    }
+    return SYMEIG_OK;
 }
 
 int symeig_batched_tuning(int64_t* split, int32_t* shape_small, int32_t* shape_large, int32_t set)
 {
-    if (!split || !shape_small || !shape_large) return SYMEIG_ERR_NULL;
-    if (set) {
-        if (*split < 1 || *shape_small < 0 || *shape_small > 1 || *shape_large < 0 || *shape_large > 1)
-            return SYMEIG_ERR_SIZE;
-        batched_set_tuning(*split, *shape_small, *shape_large);
-    } else {
-        batched_get_tuning(split, shape_small, shape_large);
-    }
-    return SYMEIG_OK;
+    return symeig_batched_tuning_dtype(1, split, shape_small, shape_large, set);
 }
 
 int symeig_eig_adjoint_f64_dev(symeig_handle h, int64_t count, int64_t n, const double* lam,

@@ -695,6 +695,7 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
     const int64_t maxiter = st->maxiter;
     const int32_t mode = st->chase_mode;
     const int32_t ms_bulges = min(max(st->ms_bulges, 2), kMaxBulges);
+    const int32_t ms_min = min(max(st->ms_min_bulges, 2), ms_bulges);
     const int64_t ms_rows = max(st->ms_rows, 4);
     int64_t iter = st->iter;
     int64_t lbe = st->last_block_ends_at;
@@ -806,6 +807,9 @@ chase_kernel(ChaseState* __restrict__ st, double* __restrict__ dv, double* __res
                                 if (exact) cap = min(cap, (int64_t)grid_layers - layer + 1);
                                 nbl = min(min((int64_t)ms_bulges, (to - from + 1) / ms_rows), cap);
                                 nbl = min(nbl, maxiter - iter + 1);
+                                // a batch too small to repay its launches and shift solve
+                                // runs as one sweep with the reference's shift
+                                if (nbl < ms_min) nbl = 1;
                             }
                             if (nbl >= 2) {
                                 batch_shifts_setup(dv, ev, from, to, (int)nbl, swin, ms_d, ms_e2, ms_ea, ms_dd, ms_ee2);

@@ -64,6 +64,8 @@ constexpr int kMaxBulges = 128;
 constexpr int kDefaultBulges = 64;
 constexpr int kDefaultRowsPerBulge = 16;
 constexpr int kDefaultProgEvery = 4;
+// A block with room for fewer than ms_min_bulges bulges takes a single sweep instead of a batch.
+constexpr int kDefaultMinBulges = 2;
 constexpr int kBatchesAhead = 8;
 
 // Device scratch of a batch: the bulges' shifts and their progress words.
@@ -108,6 +110,8 @@ struct ChaseState {
     int32_t ms_prog_mask;        // a bulge releases its progress every (mask + 1) steps
     int32_t test_stall;          // test hook (symeig_set_test_stall): bulge 0 of a batch never
                                  // releases its progress, so the next bulge's wait runs out
+    int32_t ms_min_bulges;       // fewest bulges of a batch; fewer make a single sweep (>= 2)
+    int32_t pad1;
 };
 
 // ---- launch helpers (defined in the .cu files) ------------------------------------------
@@ -228,17 +232,20 @@ cudaError_t launch_chase_batched(const BatchMat* mats, const int32_t* order, int
                                  ChaseState* states, double* d, double* e, double* grids,
                                  int32_t* thick, int32_t* place, cudaStream_t stream);
 
-// Batched solve on device pointers (batched.cu); n, converged, iters are host arrays.
+// Batched solve on device pointers (batched.cu); n, converged, iters are host arrays; Q is
+// FP64 or FP32 (the FP32-Q variant).
+template <typename T>
 int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t* n, double* d,
-                   double* e, double* Q, int32_t max_layers, double tol, int64_t maxiter_factor,
+                   double* e, T* Q, int32_t max_layers, double tol, int64_t maxiter_factor,
                    int32_t exact_order, int32_t* converged, int64_t* iters, int64_t* rounds_out,
                    double* ms_out);
-int batched_autotune(int device, cudaStream_t stream, double* ms);
+int batched_autotune(int device, cudaStream_t stream, int64_t count, const int64_t* n, double* ms);
 // Adjoint of the eigensolve for count matrices of order n (adjoint.cu).
 int adjoint_dev(cudaStream_t s, int64_t count, int64_t n, const double* lam, const double* Q,
                 const double* glam, const double* gQ, double* gd, double* ge, double* scratch);
 int64_t adjoint_scratch_doubles(int64_t count, int64_t n);
-void batched_set_tuning(int64_t split, int32_t shape0, int32_t shape1);
-void batched_get_tuning(int64_t* split, int32_t* shape0, int32_t* shape1);
+void batched_set_tuning(int fp64, int64_t split, int32_t shape0, int32_t shape1);
+void batched_get_tuning(int fp64, int64_t* split, int32_t* shape0, int32_t* shape1);
+int batched_num_tiles();
 
 }  // namespace symeig

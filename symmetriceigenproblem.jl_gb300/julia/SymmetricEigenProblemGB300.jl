@@ -102,20 +102,30 @@ function bulk_wave_order_2x2_lmul!(A::StridedMatrix{T}, givens::Matrix{Tuple{T,T
     return nothing
 end
 
-"""Many qr_algorithm! calls in one: H_i and Q_i (n_i x n_i) updated in place."""
-function qr_algorithm_batched!(Hs::Vector{SymTridiagonal{Float64,Vector{Float64}}}, Qs::Vector{Matrix{Float64}};
-                               max_layers::Int = 128, tol = eps(Float64), maxiter_factor::Int = 100)
+"""Many qr_algorithm! calls in one: H_i and Q_i (n_i x n_i) updated in place.  Q_i are all
+Float64, or all Float32 (the FP32-Q variant: the chase stays Float64)."""
+function qr_algorithm_batched!(Hs::Vector{SymTridiagonal{Float64,Vector{Float64}}}, Qs::Vector{Matrix{T}};
+                               max_layers::Int = 128, tol = eps(Float64),
+                               maxiter_factor::Int = 100) where {T<:Union{Float32,Float64}}
     ns = Int64[size(H, 1) for H in Hs]
     d = reduce(vcat, [H.dv for H in Hs])
     e = reduce(vcat, [H.ev for H in Hs])
     Q = reduce(vcat, [vec(Q) for Q in Qs])
     conv = zeros(Int32, length(Hs))
     iters = zeros(Int64, length(Hs))
-    st = ccall((:symeig_qr_batched_f64, libsymeig), Cint,
-        (Ptr{Cvoid}, Int64, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int32, Float64, Int64,
-         Ptr{Int32}, Ptr{Int64}),
-        handle(), length(Hs), ns, d, e, Q, max_layers, Float64(tol), maxiter_factor, conv, iters)
-    check(:symeig_qr_batched_f64, st)
+    if T === Float64
+        st = ccall((:symeig_qr_batched_f64, libsymeig), Cint,
+            (Ptr{Cvoid}, Int64, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int32, Float64, Int64,
+             Ptr{Int32}, Ptr{Int64}),
+            handle(), length(Hs), ns, d, e, Q, max_layers, Float64(tol), maxiter_factor, conv, iters)
+        check(:symeig_qr_batched_f64, st)
+    else
+        st = ccall((:symeig_qr_batched_f64_q32, libsymeig), Cint,
+            (Ptr{Cvoid}, Int64, Ptr{Int64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float32}, Int32, Float64, Int64,
+             Ptr{Int32}, Ptr{Int64}),
+            handle(), length(Hs), ns, d, e, Q, max_layers, Float64(tol), maxiter_factor, conv, iters)
+        check(:symeig_qr_batched_f64_q32, st)
+    end
     od = oe = oq = 0
     for (k, n) in enumerate(ns)
         Hs[k].dv .= view(d, od+1:od+n); od += n

@@ -56,6 +56,26 @@ def test_batched_packing_is_checked(pkg):
         pkg.qr_algorithm_batched_(np.zeros(7), np.zeros(5), n, np.zeros(24))   # Q has 25
     with pytest.raises(TypeError):
         pkg.qr_algorithm_batched_(np.zeros(7, dtype=np.float32), np.zeros(5), n)
+    with pytest.raises(TypeError):   # Q float16
+        pkg.qr_algorithm_batched_(np.zeros(7), np.zeros(5), n, np.zeros(25, dtype=np.float16))
+
+
+def test_batched_tuning_per_dtype(pkg):
+    """The batched tuning is kept per precision of Q; tiles 0..2 are accepted, others and a
+    split below 1 are refused (SYMEIG_ERR_SIZE) and leave the tuning unchanged.  No device."""
+    old64, old32 = pkg.batched_tuning(fp64=True), pkg.batched_tuning(fp64=False)
+    try:
+        pkg.batched_tuning(fp64=True, split=300, shape_small=2, shape_large=1)
+        pkg.batched_tuning(fp64=False, split=100, shape_small=1, shape_large=2)
+        assert pkg.batched_tuning(fp64=True) == {"split": 300, "shape_small": 2, "shape_large": 1}
+        assert pkg.batched_tuning(fp64=False) == {"split": 100, "shape_small": 1, "shape_large": 2}
+        for bad in ({"shape_small": 3}, {"shape_large": -1}, {"split": 0}):
+            with pytest.raises(pkg.SymeigError):
+                pkg.batched_tuning(fp64=True, **bad)
+        assert pkg.batched_tuning(fp64=True) == {"split": 300, "shape_small": 2, "shape_large": 1}
+    finally:
+        pkg.batched_tuning(fp64=True, **old64)
+        pkg.batched_tuning(fp64=False, **old32)
 
 
 def test_wave_port_threads_do_not_change_bits(oracle, pkg):
