@@ -226,10 +226,13 @@ int symeig_batched_autotune_sizes(symeig_handle h, int64_t count, const int64_t*
  * (fp64 != 0) or FP32: 0 = 8 lane groups of 8 layers (4 rows per warp), 1 = 4 groups of 16
  * layers (8 rows per warp); FP32 only: 2 = shape 1 and 3 = shape 0 with two rows per thread,
  * 4 = shape 1 in CTAs of 14 warps (112 rows); FP64 only: 2 = shape 0 in CTAs of 27 warps
- * (108 rows, one CTA per SM at m = 16384).  FP64 shape 0 runs as 2, and FP32 shape 2 as 4,
- * when m >= 15000.  Defaults: FP64 0, FP32 2.  Returns SYMEIG_ERR_SIZE for a shape the
- * precision lacks.
- * Process-wide.  No reference counterpart. */
+ * (108 rows, one CTA per SM at m = 16384), 3 = 16 groups of 8 layers, passes of 128 layers
+ * (2 rows per warp; canonical form, for more than 64 layers, else it runs as 0).  FP64 shape 0
+ * runs as 2, and FP32 shape 2 as 4, when m >= 15000.  -1 (the default for both) chooses by the
+ * launch's rows m: FP64 shape 3 below 7168 rows for more than 64 layers, else shape 0 below
+ * 9728 rows and 2 from there; FP32 shape 0 below 7168, 1 below 14336 and 4 from there (the
+ * fastest measured at each m).  Returns SYMEIG_ERR_SIZE for a shape the precision
+ * lacks.  Process-wide.  No reference counterpart. */
 int symeig_apply_tuning(int32_t fp64, int32_t* shape, int32_t set);
 /* Read (set = 0) or write (set != 0) the batched tuning of FP64 Q (fp64 != 0) or FP32 Q: the
  * class split and the tile (0..2, as for the autotuner) per class.  SYMEIG_ERR_SIZE for a split

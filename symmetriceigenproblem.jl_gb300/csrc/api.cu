@@ -184,7 +184,7 @@ int apply_grid(symeig_handle h, T* Q, int64_t ldq, int64_t m, const Tsrc* grid, 
                int64_t rs = 1)
 {
     if (m <= 0 || n_loc < 2 || layers <= 0) return SYMEIG_OK;
-    const int64_t per = apply_layers_per_pass<T>();
+    const int64_t per = apply_layers_per_pass<T>(m, layers, sizeof(T) == 8 ? h->apply_form : 0);
     CK(h->table.ensure(apply_table_bytes<T>(n_loc, layers)));
     // the scaled form: the column-scale recurrences of all passes at once
     bool rec_all = false;
@@ -484,8 +484,8 @@ int apply_host(symeig_handle h, T* A, int64_t lda, int64_t m, int64_t n, const T
     CK(h->q.ensure((size_t)m * n * sizeof(T)));
     const size_t cs_bytes = (size_t)(n - 1) * k * 2 * sizeof(T);
     CK(h->cs.ensure(cs_bytes));
-    if (k <= apply_layers_per_pass<T>() && m >= (int64_t)kPipeBlocks * 256 && !h->kernel_timing &&
-        apply_host_segmented_supported<T>()) {
+    if (k <= 64 && m >= (int64_t)kPipeBlocks * 256 && !h->kernel_timing &&
+        apply_host_segmented_supported<T>(m)) {
         rc = apply_host_pipelined<T>(h, A, lda, m, n, cs, k);
         if (rc) {
             // nothing queued may still read or write the caller's buffer after the return
@@ -967,7 +967,7 @@ int symeig_apply_tuning(int32_t fp64, int32_t* shape, int32_t set)
 {
     if (!shape) return SYMEIG_ERR_NULL;
     if (set) {
-        if (*shape < 0 || *shape >= apply_num_shapes(fp64)) return SYMEIG_ERR_SIZE;
+        if (*shape < -1 || *shape >= apply_num_shapes(fp64)) return SYMEIG_ERR_SIZE;
         apply_set_shape(fp64, *shape);
     } else {
         *shape = apply_get_shape(fp64);

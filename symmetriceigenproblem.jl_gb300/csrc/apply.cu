@@ -30,8 +30,8 @@ using wave::kThreads;
 //             shared memory serves two rows, so the shared-memory pipe (2 wavefronts per
 //             128-bit broadcast read of 4 or 8 distinct addresses) carries half the load per
 //             rotation-row, and each thread has two independent rotation chains.  Shape 2
-//             is the FP32 choice (1.5-3 % ahead of shape 1, measured); from 15000 rows on it
-//             runs as shape 4 (below).
+//             runs as shape 4 (below) from 15000 rows on.
+// By default (kAutoShape) the rows of the launch choose the shape (resolve_shape).
 template <typename T, int S> struct Cfg;
 // MINB: CTAs per SM the launch bounds ask for; MINB_INT the same for the FP64 kernels whose
 // products run on the integer pipes (int_mul.cuh: about 95 registers with one row per thread).
@@ -51,13 +51,18 @@ template <> struct Cfg<float, 3> { using Sh = Shape<float, 8, 8, 2>; static cons
 // CTAs of 27 warps 25.2, 8 x 8 with two rows per thread in 14 warps 24.9, four rows per
 // thread in 7 warps 24.3, 16 x 4 with two rows in 7 warps 27.6).
 template <> struct Cfg<float, 4> { using Sh = Shape<float, 16, 4, 1, 14>; static constexpr int MINB = 1, MINB_INT = 1; static constexpr int THREADS = Sh::THREADS; };
+// FP64 shape 3 = 16 lane groups of 8 layers: 128 layers per pass, 2 rows per warp.  A flush of
+// the reference's 128-layer buffer runs as one pass instead of two: twice the lane groups per
+// row (the parallelism of a short Q) and one read and write of Q instead of two.  Canonical
+// form, for passes of more than 64 layers.
+template <> struct Cfg<double, 3> { using Sh = Shape<double, 8, 16>; static constexpr int MINB = 5, MINB_INT = 5; static constexpr int THREADS = Sh::THREADS; };
 static_assert(Cfg<float, 4>::Sh::CHUNK == Cfg<float, 1>::Sh::CHUNK, "table layout");
 // the table depends on (KB, G) only, so shapes 2 and 3 share the tables of 1 and 0
 static_assert(Cfg<float, 2>::Sh::CHUNK == Cfg<float, 1>::Sh::CHUNK, "table layout");
 static_assert(Cfg<float, 3>::Sh::CHUNK == Cfg<float, 0>::Sh::CHUNK, "table layout");
 static_assert(Cfg<double, 2>::Sh::CHUNK == Cfg<double, 0>::Sh::CHUNK, "table layout");
 
-constexpr int kShapes[2] = {3, 5};  // shapes available to [0] FP64, [1] FP32
+constexpr int kShapes[2] = {4, 5};  // shapes available to [0] FP64, [1] FP32
 // FP64 shape 0 runs as shape 2 from this many rows on (about 152 SMs x 108 rows x 0.92)
 constexpr int64_t kWideRows = 15000;
 // The canonical FP64 form computes its products on the integer pipes from this many rows on.
@@ -65,8 +70,48 @@ constexpr int64_t kWideRows = 15000;
 // (measured, 64 layers on m x m: 556 against 642 GFLOP/s at m = 2000, 916 against 710 at
 // m = 4096), and the products stay on the FP64 pipe; both give the same bits.
 constexpr int64_t kIntMulRows = 3072;
-int g_shape[2] = {0, 2};            // [0] FP64, [1] FP32
-template <typename T> int shape_index() { return g_shape[sizeof(T) == 8 ? 0 : 1]; }
+// The tile shape by precision ([0] FP64, [1] FP32): a shape index, or kAutoShape (the default)
+// for the shape chosen by the rows of the launch.  Measured at n = 4096, k = 64 for m = 1024 ..
+// 16384 (TFLOP/s):
+//   FP32  m:      2048   4096   6144   8192  12288  15000  16384
+//         shape 0  8.60  15.10  18.77  19.64  19.82  21.44  23.25
+//         shape 1  6.92  13.75  16.30  21.55  24.30  22.01  23.94
+//         shape 4  3.32   6.62   9.95  13.26  19.86  24.25  26.31   (shape 2: within 8 % of 4)
+//   FP64  shape 0  0.67   0.81   0.90   0.88   0.84   1.39*  1.51*  (* as shape 2)
+//         shape 2  0.10   0.38   0.57   0.76   1.14   1.39   1.51
+// The 27-warp FP64 shape runs one CTA of 108 rows per SM, so it pays once m gives it about 90
+// of the 152 SMs; FP32 shape 0 wins while its 16-row CTAs are needed to fill the SMs, shape 1
+// in between, and the 14-warp shape 4 from about 14000 rows.
+constexpr int kAutoShape = -1;
+constexpr int64_t kAutoWideRows64 = 9728;       // FP64: shape 0 below, shape 2 from here
+constexpr int64_t kAutoRows32[2] = {7168, 14336};  // FP32: shape 0 below [0], 1 below [1], 4 from [1]
+int g_shape[2] = {kAutoShape, kAutoShape};
+
+// FP64: passes of more than 64 layers in the canonical form run as one 128-layer pass of
+// shape 3 below this many rows (auto), where the grid is short of warps.  Measured on m x m, k =
+// 128 (TFLOP/s, shape 0 as two passes against shape 3 as one): m = 1000 0.309 / 0.578, 3000
+// 0.515 / 0.669, 4096 0.823 / 0.884, 6000 0.909 / 1.037, 8192 0.906 / 0.777; equal at 2000
+// (0.641 / 0.650), where both leave a fifth of the SMs idle and saturate the FP64 pipes of the
+// rest.  Both give the same bits.
+constexpr int64_t kAutoDeepRows64 = 7168;
+
+// The shape an m-row launch of T runs for a pass of `layers` layers in `form`: the auto choice
+// above, or the tuned shape (FP64 0 runs as 2, and FP32 2 as 4, from kWideRows rows on).  The
+// 128-layer FP64 shape 3 takes only passes of more than 64 layers of canonical rotations (the
+// scaled form's recurrences run in passes of 64); others run as 0.
+template <typename T> int resolve_shape(int64_t m, int64_t layers = 64, int form = 0)
+{
+    const int s = g_shape[sizeof(T) == 8 ? 0 : 1];
+    if constexpr (sizeof(T) == 8) {
+        const bool deep_ok = layers > 64 && form != 1;   // canonical rotations (form 0 or 2)
+        if (s == kAutoShape) return (deep_ok && m < kAutoDeepRows64) ? 3 : (m < kAutoWideRows64 ? 0 : 2);
+        if (s == 3) return deep_ok ? 3 : 0;
+        return (s == 0 && m >= kWideRows) ? 2 : s;
+    } else {
+        if (s == kAutoShape) return m < kAutoRows32[0] ? 0 : (m < kAutoRows32[1] ? 1 : 4);
+        return (s == 2 && m >= kWideRows) ? 4 : s;
+    }
+}
 
 template <typename Tsrc, typename T, int S>
 __global__ void __launch_bounds__(256)
@@ -369,22 +414,31 @@ cudaError_t launch_mul_rn(int64_t count, const double* a, const double* b, doubl
     return cudaGetLastError();
 }
 
-template <typename T> int64_t apply_layers_per_pass() { return 64; }
-template int64_t apply_layers_per_pass<double>();
-template int64_t apply_layers_per_pass<float>();
-
-// bytes of the larger of the two shapes' tables (so the tuning can change between calls),
-// rounded up to 256
-template <typename T> size_t table_region(int64_t n_loc)
+// Layers per pass of an apply of `layers` layers to m rows in `form`: 128 where the 128-layer
+// FP64 shape takes it, else 64.
+template <typename T> int64_t apply_layers_per_pass(int64_t m, int64_t layers, int form)
 {
-    const size_t b = (size_t)std::max(Cfg<T, 0>::Sh::table_bytes(n_loc), Cfg<T, 1>::Sh::table_bytes(n_loc));
+    if constexpr (sizeof(T) == 8)
+        if (resolve_shape<T>(m, layers, form) == 3) return 128;
+    return 64;
+}
+template int64_t apply_layers_per_pass<double>(int64_t, int64_t, int);
+template int64_t apply_layers_per_pass<float>(int64_t, int64_t, int);
+
+// bytes of the largest of the shapes' tables for passes of `layers` layers (so the tuning can
+// change between calls), rounded up to 256
+template <typename T> size_t table_region(int64_t n_loc, int64_t layers = 64)
+{
+    size_t b = (size_t)std::max(Cfg<T, 0>::Sh::table_bytes(n_loc), Cfg<T, 1>::Sh::table_bytes(n_loc));
+    if constexpr (sizeof(T) == 8)
+        if (layers > 64) b = std::max(b, (size_t)Cfg<T, 3>::Sh::table_bytes(n_loc));
     return (b + 255) & ~(size_t)255;
 }
 
 // FP64: the scaled form's scratch follows the table, one slot per pass of `layers`
 template <typename T> size_t apply_table_bytes(int64_t n_loc, int64_t layers)
 {
-    size_t b = table_region<T>(n_loc);
+    size_t b = table_region<T>(n_loc, layers);
     if (sizeof(T) == 8 && n_loc >= 2) {
         const int64_t passes = layers > 64 ? (layers + 63) / 64 : 1;
         b += (size_t)passes * scaled_slot_bytes(n_loc);
@@ -584,15 +638,17 @@ cudaError_t apply_pass(T* Q, int64_t ldq, int64_t m, const Tsrc* grid, int64_t g
                        const int32_t* place, const ApplyPass& pass, void* table, int* err,
                        cudaStream_t stream, cudaEvent_t ev_begin, cudaEvent_t ev_end, int what)
 {
-    const int s = shape_index<T>();
+    const int s = resolve_shape<T>(m, pass.layers, pass.form);
     if constexpr (sizeof(T) == 8) {
-        // shape 0 takes the 27-warp CTAs of shape 2 once m fills every SM with them
-        if (s == 2 || (s == 0 && m >= kWideRows))
+        if (s == 2)
             return apply_pass_shape<Tsrc, T, 2>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
+                                                stream, ev_begin, ev_end, what);
+        if (s == 3)
+            return apply_pass_shape<Tsrc, T, 3>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
                                                 stream, ev_begin, ev_end, what);
     }
     if constexpr (sizeof(T) == 4) {
-        if (s == 4 || (s == 2 && m >= kWideRows))
+        if (s == 4)
             return apply_pass_shape<Tsrc, T, 4>(Q, ldq, m, grid, grid_rows, place, pass, table, err,
                                                 stream, ev_begin, ev_end, what);
         if (s == 2)
@@ -615,27 +671,28 @@ cudaError_t apply_host_segmented(T* dQ, int64_t m, const T* d_cs, const ApplyPas
 {
     if (pass.n_loc < 2 || pass.layers <= 0 || m <= 0) return cudaSuccess;
     if (pass.layers > 64 || pass.c0 != 0 || pass.L0 != 0) return cudaErrorInvalidValue;
-    // segment kernels exist for the default tile shapes only (FP64 0 and its 27-warp form 2,
-    // FP32 2 and its 14-warp form 4); other tunings take the unpipelined path
-    const int s = shape_index<T>();
+    // segmented launches exist for FP64 shapes 0 and 2 and FP32 shapes 0, 1, 2 and 4 (every
+    // shape the auto choice takes); other tunings take the unpipelined path
+    const int s = resolve_shape<T>(m);
     if constexpr (sizeof(T) == 8) {
-        if (s == 2 || (s == 0 && m >= kWideRows))
-            return host_segmented_shape<T, 2>(dQ, m, d_cs, pass, table, err, stream, io);
+        if (s == 2) return host_segmented_shape<T, 2>(dQ, m, d_cs, pass, table, err, stream, io);
         if (s == 0) return host_segmented_shape<T, 0>(dQ, m, d_cs, pass, table, err, stream, io);
     } else {
-        if (s == 4 || (s == 2 && m >= kWideRows)) return host_segmented_shape<T, 4>(dQ, m, d_cs, pass, table, err, stream, io);
+        if (s == 4) return host_segmented_shape<T, 4>(dQ, m, d_cs, pass, table, err, stream, io);
         if (s == 2) return host_segmented_shape<T, 2>(dQ, m, d_cs, pass, table, err, stream, io);
+        if (s == 1) return host_segmented_shape<T, 1>(dQ, m, d_cs, pass, table, err, stream, io);
+        if (s == 0) return host_segmented_shape<T, 0>(dQ, m, d_cs, pass, table, err, stream, io);
     }
     return cudaErrorNotSupported;
 }
-// Whether apply_host_segmented takes the current tile shape of T.
-template <typename T> bool apply_host_segmented_supported()
+// Whether apply_host_segmented takes the shape an m-row launch of T runs.
+template <typename T> bool apply_host_segmented_supported(int64_t m)
 {
-    const int s = shape_index<T>();
-    return sizeof(T) == 8 ? (s == 0 || s == 2) : (s == 2 || s == 4);
+    const int s = resolve_shape<T>(m);
+    return sizeof(T) == 8 ? (s == 0 || s == 2) : (s != 3);
 }
-template bool apply_host_segmented_supported<double>();
-template bool apply_host_segmented_supported<float>();
+template bool apply_host_segmented_supported<double>(int64_t);
+template bool apply_host_segmented_supported<float>(int64_t);
 template cudaError_t apply_host_segmented<double>(double*, int64_t, const double*, const ApplyPass&, void*, int*,
                                                   cudaStream_t, const HostStream&);
 template cudaError_t apply_host_segmented<float>(float*, int64_t, const float*, const ApplyPass&, void*, int*,
@@ -663,7 +720,7 @@ template size_t apply_segment_state_bytes<float>(int64_t);
 int apply_num_shapes(int fp64) { return kShapes[fp64 ? 0 : 1]; }
 void apply_set_shape(int fp64, int shape)
 {
-    g_shape[fp64 ? 0 : 1] = (shape >= 0 && shape < apply_num_shapes(fp64)) ? shape : 0;
+    g_shape[fp64 ? 0 : 1] = (shape >= 0 && shape < apply_num_shapes(fp64)) ? shape : kAutoShape;
 }
 int apply_get_shape(int fp64) { return g_shape[fp64 ? 0 : 1]; }
 

@@ -98,7 +98,7 @@ extern "C" int symeig_apply_givens_f64_noalloc(double* A, int64_t lda, int64_t m
     if (m > 0 && lda < m) return SYMEIG_ERR_LD;
     if (m == 0 || n < 2 || k == 0) return SYMEIG_OK;
     if (!cs) return SYMEIG_ERR_NULL;
-    const int64_t per = apply_layers_per_pass<double>();
+    const int64_t per = 64;   // passes of the 64-layer tiles, whose tables the scratch holds
     if (apply_canonical_table_bytes<double>(n) > (size_t)SYMEIG_NOALLOC_SCRATCH_BYTES) return SYMEIG_ERR_SIZE;
     void* table = nullptr;
     int* err = nullptr;

@@ -141,7 +141,9 @@ cudaError_t launch_scaled_recurrences(const double* grid, int64_t grid_rows, con
                                       void* table, cudaStream_t stream);
 
 // Layers one pass of the wave-window kernel handles for element type T.
-template <typename T> int64_t apply_layers_per_pass();
+// Layers per pass of an apply of `layers` layers to m rows in `form` (64, or 128 where the
+// 128-layer FP64 tile takes the pass).
+template <typename T> int64_t apply_layers_per_pass(int64_t m, int64_t layers, int form);
 
 // Bytes of the wave table one pass needs (for FP64 including the scaled form's scratch).
 template <typename T> size_t apply_table_bytes(int64_t n_loc, int64_t layers);
@@ -180,7 +182,7 @@ template <typename T>
 cudaError_t apply_host_segmented(T* dQ, int64_t m, const T* d_cs, const ApplyPass& pass, void* table, int* err,
                                  cudaStream_t stream, const HostStream& io);
 template <typename T> size_t apply_segment_state_bytes(int64_t m);
-template <typename T> bool apply_host_segmented_supported();
+template <typename T> bool apply_host_segmented_supported(int64_t m);
 
 // Tile shape of the single-matrix wave kernel per precision (see apply.cu).
 void apply_set_shape(int fp64, int shape);

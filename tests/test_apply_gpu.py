@@ -49,14 +49,16 @@ def test_apply_host_buffers_with_leading_dimension(cuda, pkg, oracle, dtype):
 @pytest.mark.parametrize("dtype", [np.float64, np.float32])
 @pytest.mark.parametrize("m,n,k,ld", [(4100, 300, 64, 4100), (4099, 129, 40, 4111), (4096, 70, 1, 4096),
                                       (5000, 200, 65, 5000), (2100, 90, 64, 2100), (4096, 2001, 64, 4096),
-                                      (15360, 600, 64, 15363), (4097, 3, 2, 4097), (4096, 2, 64, 4096)])
+                                      (15360, 600, 64, 15363), (4097, 3, 2, 4097), (4096, 2, 64, 4096),
+                                      (8200, 150, 64, 8201), (10001, 97, 33, 10001)])
 def test_apply_host_pipelined_column_segments(cuda, pkg, oracle, m, n, k, ld, dtype):
     """Host Q with k <= 64 and m >= 4096 runs as 16 launches over column segments of one pass
     (copies in, kernels and copies out on three streams; each launch carries its registers to
     the next through a state buffer): the result is the oracle's bits, and the rows beyond m of
     a leading dimension are untouched.  Small n gives one table chunk per segment (every
-    boundary a segment boundary); m = 15360 takes the 27-warp FP64 shape.  k = 65 and
-    m = 2100 take the unpipelined path."""
+    boundary a segment boundary).  The default tile choice by rows takes FP64 shape 0 below
+    9728 rows and the 27-warp shape 2 above, FP32 shape 0 below 7168, 1 up to 14336 (m = 8200,
+    10001) and 4 above.  k = 65 and m = 2100 take the unpipelined path."""
     rng = np.random.default_rng(m + n + k)
     big = np.asfortranarray((rng.random((ld, n)) * 2 - 1).astype(dtype))
     A = big[:m, :]
@@ -69,14 +71,20 @@ def test_apply_host_pipelined_column_segments(cuda, pkg, oracle, m, n, k, ld, dt
     assert np.array_equal(big[m:, :], untouched)
 
 
-@pytest.mark.parametrize("m", [15000, 15500, 16417])
-def test_apply_wide_ctas_for_tall_q(cuda, pkg, oracle, m):
-    """From 15000 rows on, FP64 tile shape 0 runs in CTAs of 27 warps (one per SM at 16384
-    rows); the last CTA is partial.  Bits as the oracle's, device path."""
-    rng = np.random.default_rng(m)
-    n, k = 40, 64
-    g = rotation_grid(pkg, rng, n, k, np.float64)
-    A = np.asfortranarray(rng.random((m, n)) * 2 - 1)
+@pytest.mark.parametrize("dtype", [np.float64, np.float32])
+@pytest.mark.parametrize("m,k", [(7167, 64), (7168, 64), (9727, 64), (9728, 64), (14335, 64), (14336, 64),
+                                 (15000, 64), (15500, 64), (16417, 64), (1000, 128), (3071, 128), (3072, 96),
+                                 (7167, 128), (7168, 128)])
+def test_apply_auto_shape_by_rows(cuda, pkg, oracle, m, k, dtype):
+    """The default tile choice by rows, on each side of its thresholds: FP64 shape 0 below 9728
+    rows, CTAs of 27 warps (one per SM at 16384 rows) from there, and below 7168 rows one pass
+    of 128 layers (shape 3) for more than 64 layers, with the integer-pipe products from 3072
+    rows; FP32 shape 0 below 7168, 1 below 14336, CTAs of 14 warps from there.  The last CTA
+    is partial.  Bits as the oracle's, device path."""
+    rng = np.random.default_rng(m + k)
+    n = 40
+    g = rotation_grid(pkg, rng, n, k, dtype)
+    A = np.asfortranarray((rng.random((m, n)) * 2 - 1).astype(dtype))
     ref = A.copy(order="F")
     oracle.apply_seq(ref, g)
     dA = to_device_colmajor(cuda, A)
@@ -112,12 +120,15 @@ def test_left_apply_matches_oracle(cuda, pkg, oracle, m, n, k, dtype):
     assert np.array_equal(B, refT.T)
 
 
-@pytest.mark.parametrize("dtype,shape", [(np.float64, 0), (np.float64, 1), (np.float64, 2), (np.float32, 0),
-                                         (np.float32, 1), (np.float32, 2), (np.float32, 3), (np.float32, 4)])
+@pytest.mark.parametrize("dtype,shape", [(np.float64, 0), (np.float64, 1), (np.float64, 2), (np.float64, 3),
+                                         (np.float32, 0), (np.float32, 1), (np.float32, 2), (np.float32, 3),
+                                         (np.float32, 4)])
 def test_apply_every_tile_shape(cuda, pkg, oracle, dtype, shape):
     """Every tile shape of the single-matrix wave kernel gives the oracle's bits (FP32 shapes 2
     and 3 hold two rows per thread, FP32 shape 4 is a CTA of 14 warps, FP64 shape 2 one of 27
-    warps; the row counts leave partial tiles and partial warps)."""
+    warps, FP64 shape 3 runs passes of 128 layers -- k = 130 is one such pass and a 2-layer pass
+    in shape 0, k = 100 one pass of 100 layers; the row counts leave partial tiles and partial
+    warps)."""
     import ctypes
     lib = pkg.load_library()
     fp64 = int(dtype == np.float64)
@@ -127,7 +138,8 @@ def test_apply_every_tile_shape(cuda, pkg, oracle, dtype, shape):
     assert lib.symeig_apply_tuning(fp64, ctypes.byref(v), 1) == 0
     try:
         rng = np.random.default_rng(99 + shape)
-        for (m, n, k) in [(33, 70, 64), (100, 129, 130), (7, 20, 5), (77, 40, 64), (333, 90, 64), (15100, 50, 64)]:
+        for (m, n, k) in [(33, 70, 64), (100, 129, 130), (7, 20, 5), (77, 40, 64), (333, 90, 64), (15100, 50, 64),
+                          (3100, 60, 100)]:
             g = rotation_grid(pkg, rng, n, k, dtype)
             A = np.asfortranarray((rng.random((m, n)) * 2 - 1).astype(dtype))
             ref = A.copy(order="F")

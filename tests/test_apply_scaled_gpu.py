@@ -39,7 +39,7 @@ def test_scaled_apply_matches_oracle(cuda, pkg, oracle, shape, m, n, k):
         dA = to_device_colmajor(cuda, Q0)
         pkg.bulk_wave_order_2x2_rmul_(dA, cuda.from_numpy(cs).cuda(), form=1)
     finally:
-        _set_shape(pkg, 0)
+        _set_shape(pkg, -1)
     assert np.array_equal(A, ref)
     assert np.array_equal(dA.cpu().numpy(), ref)
     canon = Q0.copy(order="F")

@@ -137,21 +137,22 @@ def test_dense_entry_points_validate_arguments(pkg):
 
 
 def test_apply_tuning_shapes_per_precision(pkg):
-    """symeig_apply_tuning keeps the tile shape per precision: FP64 has shapes 0-2 (2: one CTA
-    of 27 warps), FP32 0-4 (2 and 3 hold two rows per thread, 4 is a CTA of 14 warps);
-    out-of-range shapes are refused and leave it as it was.  Setting the shape touches no
-    device."""
+    """symeig_apply_tuning keeps the tile shape per precision: FP64 has shapes 0-3 (2: one CTA
+    of 27 warps, 3: passes of 128 layers), FP32 0-4 (2 and 3 hold two rows per thread, 4 is a CTA of 14 warps), and -1
+    (the default) chooses by the rows of each launch; out-of-range shapes are refused and
+    leave it as it was.  Setting the shape touches no device."""
     import ctypes
     lib = pkg.load_library()
     v = ctypes.c_int32()
-    assert lib.symeig_apply_tuning(1, ctypes.byref(v), 0) == 0 and v.value == 0
-    assert lib.symeig_apply_tuning(0, ctypes.byref(v), 0) == 0 and v.value == 2
-    for fp64, bad in ((1, 3), (1, -1), (0, 5)):
+    assert lib.symeig_apply_tuning(1, ctypes.byref(v), 0) == 0 and v.value == -1
+    assert lib.symeig_apply_tuning(0, ctypes.byref(v), 0) == 0 and v.value == -1
+    for fp64, bad in ((1, 4), (1, -2), (0, 5)):
         v = ctypes.c_int32(bad)
         assert lib.symeig_apply_tuning(fp64, ctypes.byref(v), 1) == 2      # SYMEIG_ERR_SIZE
     v = ctypes.c_int32(3)
     assert lib.symeig_apply_tuning(0, ctypes.byref(v), 1) == 0
     assert lib.symeig_apply_tuning(0, ctypes.byref(v), 0) == 0 and v.value == 3
-    v = ctypes.c_int32(2)
+    v = ctypes.c_int32(-1)
     assert lib.symeig_apply_tuning(0, ctypes.byref(v), 1) == 0
-    assert lib.symeig_apply_tuning(1, ctypes.byref(v), 0) == 0 and v.value == 0
+    assert lib.symeig_apply_tuning(0, ctypes.byref(v), 0) == 0 and v.value == -1
+    assert lib.symeig_apply_tuning(1, ctypes.byref(v), 0) == 0 and v.value == -1

@@ -119,9 +119,10 @@ def test_apply_forms_bit_exact(cuda, pkg, oracle, m, n, k, form):
     assert np.array_equal(dA.cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("shape", [0, 1, 2])
+@pytest.mark.parametrize("shape", [0, 1, 2, 3])
 def test_apply_fp64_tile_shapes_bit_exact(cuda, pkg, oracle, shape):
-    """Every FP64 tile shape (symeig_apply_tuning) with the integer-pipe products."""
+    """Every FP64 tile shape (symeig_apply_tuning) with the integer-pipe products (shape 3 with
+    k = 17 runs as shape 0; with k = 100 as one 128-layer pass)."""
     torch = cuda
     lib = pkg.load_library()
     old = ctypes.c_int32()
@@ -130,7 +131,7 @@ def test_apply_fp64_tile_shapes_bit_exact(cuda, pkg, oracle, shape):
     assert lib.symeig_apply_tuning(1, ctypes.byref(sh), 1) == 0
     try:
         rng = np.random.default_rng(shape)
-        for (m, n, k) in [(1000, 200, 64), (16384, 40, 17)]:
+        for (m, n, k) in [(1000, 200, 64), (16384, 40, 17), (4000, 50, 100)]:
             g = rotation_grid(pkg, rng, n, k)
             A = np.asfortranarray(rng.random((m, n)) * 2 - 1)
             ref = A.copy(order="F")
