@@ -14,7 +14,8 @@
 //   * H = floor(P / 2^42), a 64-bit integer in [2^62, 2^64), with every nonzero bit of
 //     P mod 2^42 folded into H's bit 0 (a sticky bit: H's bits 0..8 lie below the rounding
 //     position in either case, so only their being nonzero matters).
-//   * The rounding position: k = 11 if H >= 2^63 (P >= 2^105) else 10.  Round to nearest even:
+//   * The rounding position: k = 11 if H >= 2^63 (P >= 2^105) else 10.  Round to nearest even
+//     (the sticky bit in H's bit 0, below the rounding position):
 //     M = (H + 2^(k-1) - 1 + bit_k(H)) >> k, a 53-bit significand, or 2^53 when the rounding
 //     carries out (then the exponent field below is one too small and adding M's implicit
 //     bit position carries into it, which gives the right bits, up to an overflow to infinity).
@@ -69,7 +70,7 @@ __device__ __forceinline__ double mul_rn_int(const SplitFactor& f, double y, boo
     // the implicit bit only for a nonzero exponent field: y = +-0 gives P = 0 (a subnormal y
     // gives garbage, flagged special below)
     const uint32_t y1 = (yh & 0x000FFFFFu) | min(ey, 0x00100000u);
-    const bool zero = f.zero || (((yh & 0x7FFFFFFFu) | yl) == 0u);
+    const bool yzero = (y1 | yl) == 0u;   // +-0 (a subnormal y keeps mantissa bits)
     // P = t3 2^64 + t2l 2^32 + t0l
     const uint64_t t0 = (uint64_t)yl * f.m0;
     const uint64_t t1 = (uint64_t)yl * f.m1 + (t0 >> 32);
@@ -77,25 +78,27 @@ __device__ __forceinline__ double mul_rn_int(const SplitFactor& f, double y, boo
     const uint64_t t3 = (uint64_t)y1 * f.m1 + (t2 >> 32);
     const uint32_t t2l = (uint32_t)t2, t0l = (uint32_t)t0;
     const uint32_t t3l = (uint32_t)t3, t3h = (uint32_t)(t3 >> 32);
-    // H = P >> 42 (hhi:hlo); the bits of P below 2^42 matter only through being nonzero
-    const uint32_t hlo = __funnelshift_r(t2l, t3l, 10);
+    // H = P >> 42 (hhi:hlo), with every nonzero bit of P below 2^42 folded into H's bit 0:
+    // H's bits 0..9 lie below the rounding position (bit 10 or 11), so only their being
+    // nonzero matters
+    const uint32_t hlo = __funnelshift_r(t2l, t3l, 10) | (((t2l & 0x3FFu) | t0l) != 0u ? 1u : 0u);
     const uint32_t hhi = __funnelshift_r(t3l, t3h, 10);
     const uint32_t big = hhi >> 31;                   // P >= 2^105: round at bit 11, else 10
     const uint32_t k = 10u + big;
-    // Round to nearest even: add 2^(k-1) - 1 + inc and drop k bits, where inc = 1 if the kept
-    // part is odd or anything below H's bit 0 is nonzero.  The latter decides only when H's
-    // dropped bits are exactly 2^(k-1) (a tie in H, which the sticky bits then break upward);
-    // in every other case adding 1 does not change the carry.  P = 0 gives M = 0.
-    const uint32_t sticky = min((t2l & 0x3FFu) | t0l, 1u);
-    const uint32_t inc = ((hlo >> k) | sticky) & 1u;
+    // Round to nearest even: add 2^(k-1) - 1 + bit_k(H) and drop k bits.  The dropped part
+    // (with the sticky bit in bit 0) carries exactly when it exceeds half an ulp, or equals it
+    // with an odd kept part.  P = 0 gives M = 0.
     const uint32_t half = 0x1FFu + (big << 9);        // 2^(k-1) - 1
-    const uint64_t Hs = (((uint64_t)hhi << 32) | hlo) + (uint64_t)(half + inc);
+    const uint64_t Hs = (((uint64_t)hhi << 32) | hlo) + (uint64_t)(half + ((hlo >> k) & 1u));
     const uint32_t slo = (uint32_t)Hs, shi = (uint32_t)(Hs >> 32);
     const uint32_t mlo = __funnelshift_r(slo, shi, k);
     const uint32_t mhi = shi >> k;
     // (E - 1) << 20, modulo 2^32; 0 for a zero factor, so that the result is the signed zero
+    const bool zero = f.zero || yzero;
     const uint32_t ef = zero ? 0u : ey + f.eadj + (big << 20);
-    special = special || (ef > (2045u << 20)) || (ey == 0x7FF00000u) || (ey == 0u && !zero);
+    // special: a result exponent out of [1, 2046] (the unsigned compare catches E - 1 < 0 as
+    // well), or y subnormal, infinite or NaN (field 0 with mantissa bits, or 2047)
+    special = special || (ef > (2045u << 20)) || (!yzero && (ey - 0x00100000u) >= 0x7FE00000u);
     const uint32_t rh = ef + mhi + ((yh & 0x80000000u) ^ f.sign);
     return __hiloint2double((int)rh, (int)mlo);
 }
