@@ -629,6 +629,12 @@ def measure_solve(pkg, n, case, q="f64", chase_mode=3, form="canonical", ms=(64,
                       "orth_over_bound": orth / (10 * n * eps)},
            "lapack_eigvals": {"seconds": round(t_lapack, 3), "cores": os.cpu_count(),
                               "kind": "scipy eigh_tridiagonal, eigenvalues only (no vectors), host"}}
+    if q == "f32":
+        # the FP32-Q variant's Q is held to the FP32 bound 10 n eps32 (its eigenvalues come from
+        # the FP64 chase and keep the FP64 bound)
+        eps32 = float(np.finfo(np.float32).eps)
+        out["errors"].update({"bound_10n_eps32": 10 * n * eps32, "resid_over_bound_eps32": resid / (10 * n * eps32),
+                              "orth_over_bound_eps32": orth / (10 * n * eps32)})
     if clk:
         out["clocks"] = clk.summary()
     return out
