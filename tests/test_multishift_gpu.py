@@ -178,3 +178,42 @@ def test_multishift_maxiter(cuda, pkg):
     lam, Q, conv, it, st = solve(pkg, d, e, Q=None, maxiter=10)
     assert not conv
     assert it <= 11
+
+
+@pytest.mark.parametrize("min_bulges", [4, 8, 64])
+def test_multishift_min_bulges(cuda, pkg, oracle, min_bulges):
+    """symeig_set_multishift_min: a block with room for fewer bulges takes a single sweep with
+    the reference's shift instead of a batch.  The solve stays within the reference's bounds,
+    runs fewer batches than with the default minimum of 2 (none when no block has room for the
+    minimum), and the oracle's restatement of the same rule also converges with fewer batches."""
+    n = 640
+    d, e = tridiag("A", n, seed=21)
+    lam0, Q0, conv0, _, st0 = solve(pkg, d, e)
+    h = pkg.Handle(0)
+    h.set_multishift_min(min_bulges)
+    H = pkg.SymTridiagonal(d.copy(), e.copy())
+    Q = np.asfortranarray(np.eye(n))
+    try:
+        _, conv, it = pkg.qr_algorithm_(H, Q, handle=h, chase_mode=3)
+        st = h.stats()
+    finally:
+        h.close()
+    assert conv0 and conv and st["device_errors"] == 0
+    assert st["bulge_batches"] < st0["bulge_batches"]
+    if min_bulges > n // 16:
+        assert st["bulge_batches"] == 0
+    eig, res, orth = errors(d, e, H.dv, Q)
+    assert eig < 1 and res < 1 and orth < 1, (eig, res, orth)
+    r2 = oracle.qr_multishift(d.copy(), e.copy(), None)
+    rm = oracle.qr_multishift(d.copy(), e.copy(), None, ms_min=min_bulges)
+    assert r2[0] and rm[0] and rm[4] < r2[4]
+
+
+def test_multishift_min_bulges_refused(cuda, pkg):
+    h = pkg.Handle(0)
+    try:
+        for bad in (1, 129):
+            with pytest.raises(pkg.SymeigError):
+                h.set_multishift_min(bad)
+    finally:
+        h.close()

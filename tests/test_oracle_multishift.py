@@ -121,6 +121,31 @@ def test_multishift_maxiter(oracle):
 
 def test_multishift_arguments_are_checked(oracle):
     d, e = tridiag("C", 50, 1)
-    for bad in (dict(ms_bulges=1), dict(ms_bulges=129), dict(ms_rows=3), dict(ms_window=0), dict(ms_window=5)):
+    for bad in (dict(ms_bulges=1), dict(ms_bulges=129), dict(ms_rows=3), dict(ms_window=0), dict(ms_window=5),
+                dict(ms_min=1), dict(ms_min=65)):
         with pytest.raises(RuntimeError):
             oracle.qr_multishift(d.copy(), e.copy(), None, **bad)
+
+
+def test_multishift_min_bulges_trades_batches_for_sweeps(oracle):
+    """A minimum batch size sends short blocks to single sweeps with the reference's shift:
+    fewer batches, the same eigenvalues within the bounds, and with a minimum above every
+    block's room no batch at all (then the chase is the reference's)."""
+    from scipy.linalg import eigh_tridiagonal
+    n = 800
+    d = np.arange(1, n + 1, dtype=np.float64)
+    e = np.random.default_rng(0).random(n - 1)
+    ref = eigh_tridiagonal(d, e, eigvals_only=True)
+    batches = {}
+    for mn in (2, 8, 64):
+        dd, ee = d.copy(), e.copy()
+        conv, it, _, rot, bat = oracle.qr_multishift(dd, ee, None, ms_min=mn)
+        assert conv
+        assert np.max(np.abs(np.sort(dd) - ref)) < 10 * n * np.finfo(float).eps * np.max(np.abs(ref))
+        batches[mn] = bat
+    assert batches[2] > batches[8] > batches[64] == 0
+    dd, ee = d.copy(), e.copy()
+    c0, it0, _, _ = oracle.qr_algorithm(dd, ee, None)
+    d64, e64 = d.copy(), e.copy()
+    conv, it, _, _, _ = oracle.qr_multishift(d64, e64, None, ms_min=64)
+    assert c0 and conv and it == it0 and np.array_equal(d64, dd)
