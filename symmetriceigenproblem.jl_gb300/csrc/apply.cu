@@ -18,11 +18,12 @@ namespace {
 using wave::Shape;
 using wave::kThreads;
 
-// Tile shapes.  Both cover 64 layers per pass.
+// Tile shapes.  Each covers 64 layers per pass, except FP64 shape 3 (128).
 //   shape 0 = 8 lane groups of 8 layers: 4 rows per warp -- at m = 16384, 4096 warps, all
 //             resident at <= 7 CTAs of 4 warps per SM (register budget 73), 6 or 7 warps per
-//             SM sub-partition.  The FP64 choice: the FP64 unit (2 FMA per SM per clock on
-//             GB300) is the limit and this shape balances it best.
+//             SM sub-partition.  The FP64 shape below 9728 rows: the FP64 unit (2 FMA per SM
+//             per clock on GB300) is the limit and this shape balances it best; from there
+//             its CTAs of 27 warps (shape 2) even out the SMs' loads.
 //   shape 1 = 4 lane groups of 16 layers: 8 rows per warp, twice the rotations per wave for
 //             the same per-wave overhead (shuffle, Q load/store, address arithmetic).  For
 //             FP32 the overhead per rotation matters more than the coarser balance.

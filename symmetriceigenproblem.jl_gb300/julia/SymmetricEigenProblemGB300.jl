@@ -18,7 +18,8 @@ and three additions without a reference counterpart:
     bulk_wave_order_2x2_lmul!(A, givens)                      # bulk form of lmul!, src/simple_givens.jl:38
     get_rotation(f, g) -> (c, s, r), elementwise               # src/simple_givens.jl:20
     syev!(A) -> (lam, V): dense symmetric eigensolve (sytrd, orgtr, qr_algorithm!)
-    set_apply_form!(form), set_chase_mode!(mode), set_multishift!(bulges, rows, release):
+    set_apply_form!(form), set_chase_mode!(mode), set_multishift!(bulges, rows, release),
+    set_multishift_min!(bulges):
         the library's arithmetic options (chase mode 3 is the multishift chase)
 
 Q may be Matrix{Float64} or Matrix{Float32} (the FP32-Q variant: FP64 chase, (c,s) rounded to
@@ -209,6 +210,12 @@ set_chase_mode!(mode::Integer) =
 set_multishift!(bulges::Integer = 64, rows::Integer = 16, release::Integer = 4) =
     check(:symeig_set_multishift, ccall((:symeig_set_multishift, libsymeig), Cint,
           (Ptr{Cvoid}, Int32, Int32, Int32), handle(), bulges, rows, release))
+
+"""Fewest bulges of a chase-mode-3 batch (2..128, default 2): a block with room for fewer takes
+single sweeps with the reference's shift."""
+set_multishift_min!(bulges::Integer = 2) =
+    check(:symeig_set_multishift_min, ccall((:symeig_set_multishift_min, libsymeig), Cint,
+          (Ptr{Cvoid}, Int32), handle(), bulges))
 
 function eigen_decomp!(H::SymTridiagonal{Float64})
     n = size(H, 1)
