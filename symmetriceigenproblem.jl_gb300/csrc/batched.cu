@@ -2,18 +2,20 @@
 // SymTridiagonal matrices of different orders) in one stream of persistent launches.
 //
 // The reference solves one matrix per call (src/bulge_chasing.jl:146).  A batch here runs
-// in rounds; each round is one flush of every unfinished matrix and is captured once as a
-// CUDA graph that is replayed until no matrix is left:
+// in rounds; each round is one flush of every unfinished matrix:
 //   1. chase: one lane per matrix runs the reference's inner loop until its rotation buffer
 //      is full or it converges (chase.cu, chase_batched_kernel).  Lanes are assigned in
 //      order of decreasing n so that a warp's 32 chases sweep similar lengths.
 //   2. worklist (one CTA): for every matrix with rotations, the column range and layer
 //      count of its flush, its number of row tiles, and exclusive prefix sums of tiles per
-//      (pass, size class) -- the work queue of (matrix, row-tile) items.
+//      (pass, size class) -- the work queue of (matrix, row-tile) items -- and the number of
+//      matrices still active.
 //   3. per pass: one CTA per matrix builds the wave table; then a persistent wave kernel per
 //      size class (grid = SMs x resident CTAs) pulls (matrix, row-tile) items from the
 //      queue with an atomic counter and runs the wave tile of wave_common.cuh on them.
-//   4. the number of unfinished matrices is copied to pinned host memory.
+// Round r's apply (3) runs beside round r + 1's chase (1), with the rotation grids double
+// buffered, and each round's work list, apply and next chase are captured once as a CUDA
+// graph (one per buffer parity) that is replayed until no matrix is left.
 // Q is FP64 (the canonical rotation with its products on the integer pipes) or FP32 (the
 // FP32-Q variant: the chase stays FP64, each (c,s) is rounded to float).  The tile -- rows per
 // tile and layers per pass (k) -- is chosen per size class and per precision of Q by the
@@ -352,9 +354,9 @@ int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t
     ChaseState* d_states = nullptr;
     int32_t* d_order = nullptr;
     int32_t* d_shape = nullptr;
-    double* d_grids = nullptr;
+    double* d_grids[2] = {nullptr, nullptr};
     int32_t* d_thick = nullptr;
-    int32_t* d_place = nullptr;
+    int32_t* d_place[2] = {nullptr, nullptr};
     Work* d_work = nullptr;
     int64_t* d_toff = nullptr;
     int64_t* d_prefix = nullptr;
@@ -362,8 +364,10 @@ int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t
     unsigned char* d_tables = nullptr;
     int* d_err = nullptr;
     Worklist* h_wl = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
+    cudaGraph_t graph[2] = {nullptr, nullptr};
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     int64_t rounds = 0;
     const bool want_q = Q != nullptr;
     int sms = 0;
@@ -372,9 +376,14 @@ int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t
     CKB(cudaMalloc(&d_states, sizeof(ChaseState) * count));
     CKB(cudaMalloc(&d_order, sizeof(int32_t) * count));
     CKB(cudaMalloc(&d_shape, sizeof(int32_t) * kClasses));
-    CKB(cudaMalloc(&d_grids, sizeof(double) * goff));
+    for (int b = 0; b < 2; ++b) {
+        CKB(cudaMalloc(&d_grids[b], sizeof(double) * goff));
+        CKB(cudaMalloc(&d_place[b], sizeof(int32_t) * doff));
+    }
     CKB(cudaMalloc(&d_thick, sizeof(int32_t) * doff));
-    CKB(cudaMalloc(&d_place, sizeof(int32_t) * doff));
+    CKB(cudaStreamCreateWithFlags(&side, cudaStreamNonBlocking));
+    CKB(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+    CKB(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
     CKB(cudaMalloc(&d_work, sizeof(Work) * count));
     CKB(cudaMalloc(&d_toff, sizeof(int64_t) * count));
     CKB(cudaMalloc(&d_prefix, sizeof(int64_t) * kMaxPasses * kClasses * (count + 1)));
@@ -390,20 +399,33 @@ int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t
     CKB(cudaStreamSynchronize(stream));
 
     {
-        // capture one round
-        CKB(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
-        {
-            cudaError_t ce = launch_chase_batched(d_mats, d_order, (int32_t)count, d_states, d, e,
-                                                  d_grids, d_thick, d_place, stream);
+        // Rounds are pipelined: round r's apply (its rotations in grid buffer r % 2) runs beside
+        // round r + 1's chase (into the other buffer).  The chase never reads Q and the apply
+        // never reads the chase states: the work list snapshots round r's flushes before the
+        // next chase starts.  The lane-per-matrix chase is as long as the batch's largest
+        // sweeps and holds few warps, the apply fills the GPU, so the two overlap well.
+        // Round 0's chase runs first; graph b (b = r % 2) then runs, per round r,
+        //   work list (round r) -> [ tables + wave passes on buffer b  ||  chase into buffer 1-b ]
+        // and copies the number of matrices still active after chase r to the host.  The loop
+        // ends at the first round with none: its chase (of converged matrices) returns at once.
+        CKB(launch_chase_batched(d_mats, d_order, (int32_t)count, d_states, d, e, d_grids[0], d_thick,
+                                 d_place[0], stream));
+        for (int b = 0; b < 2; ++b) {
+            CKB(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
             worklist_kernel<T><<<1, 1024, 0, stream>>>(d_mats, d_states, (int32_t)count, d_shape, d_work,
                                                        d_toff, d_prefix, d_wl);
+            cudaEventRecord(ev_fork, stream);
+            cudaStreamWaitEvent(side, ev_fork, 0);
+            cudaError_t ce = launch_chase_batched(d_mats, d_order, (int32_t)count, d_states, d, e,
+                                                  d_grids[1 - b], d_thick, d_place[1 - b], side);
+            cudaEventRecord(ev_join, side);
             if (want_q) {
                 // passes of 64-layer tiles: up to kMaxPasses; of the 128-layer tile: half as many
                 const int passes = std::max(tile_layers(tun.shape[0]) == 64 ? kMaxPasses : kMaxPasses / 2,
                                             tile_layers(tun.shape[1]) == 64 ? kMaxPasses : kMaxPasses / 2);
                 for (int p = 0; p < passes; ++p) {
                     batched_table_kernel<T><<<(unsigned)count, 256, 0, stream>>>(
-                        d_mats, d_work, d_toff, d_shape, d_grids, d_place, d_tables, p);
+                        d_mats, d_work, d_toff, d_shape, d_grids[b], d_place[b], d_tables, p);
                     for (int c = 0; c < kClasses; ++c) {
                         if (p >= (tile_layers(tun.shape[c]) == 64 ? kMaxPasses : kMaxPasses / 2)) continue;
                         const int64_t* pre = d_prefix + ((int64_t)p * kClasses + c) * (count + 1);
@@ -412,15 +434,16 @@ int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t
                     }
                 }
             }
+            cudaStreamWaitEvent(stream, ev_join, 0);
             cudaMemcpyAsync(h_wl, d_wl, sizeof(Worklist), cudaMemcpyDeviceToHost, stream);
-            cudaError_t end = cudaStreamEndCapture(stream, &graph);
+            cudaError_t end = cudaStreamEndCapture(stream, &graph[b]);
             if (ce != cudaSuccess) { rc = cuda_status(ce); goto done; }
             CKB(end);
             CKB(cudaGetLastError());
+            CKB(cudaGraphInstantiate(&exec[b], graph[b], 0));
         }
-        CKB(cudaGraphInstantiate(&exec, graph, 0));
         for (;;) {
-            CKB(cudaGraphLaunch(exec, stream));
+            CKB(cudaGraphLaunch(exec[rounds & 1], stream));
             CKB(cudaStreamSynchronize(stream));
             rounds += 1;
             if (h_wl->active == 0) break;
@@ -436,10 +459,20 @@ int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t
         }
     }
 done:
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
+    for (int b = 0; b < 2; ++b) {
+        if (exec[b]) cudaGraphExecDestroy(exec[b]);
+        if (graph[b]) cudaGraphDestroy(graph[b]);
+        cudaFree(d_grids[b]);
+        cudaFree(d_place[b]);
+    }
+    if (side) {
+        cudaStreamSynchronize(side);
+        cudaStreamDestroy(side);
+    }
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_join) cudaEventDestroy(ev_join);
     cudaFree(d_mats); cudaFree(d_states); cudaFree(d_order); cudaFree(d_shape);
-    cudaFree(d_grids); cudaFree(d_thick); cudaFree(d_place); cudaFree(d_work); cudaFree(d_toff);
+    cudaFree(d_thick); cudaFree(d_work); cudaFree(d_toff);
     cudaFree(d_prefix); cudaFree(d_wl); cudaFree(d_tables); cudaFree(d_err);
     if (h_wl) cudaFreeHost(h_wl);
     if (rounds_out) *rounds_out = rounds;
