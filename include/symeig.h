@@ -192,8 +192,9 @@ int symeig_apply_givens_f32_dev(symeig_handle h, float* A, int64_t lda, int64_t 
  * Q[sum_{j<i} n_j^2 ...]; Q may be NULL (eigenvalues only).  n, converged and iters are host
  * arrays of count entries.  The reference has no batched entry point; this replaces a loop of
  * qr_algorithm! calls.  Matrices run one flush per round: a one-lane-per-matrix chase, then
- * a persistent wave-kernel launch over a device-built queue of (matrix, row tile) items; one
- * round is captured as a CUDA graph and replayed until every matrix has finished. */
+ * a persistent wave-kernel launch over a device-built queue of (matrix, row tile) items.  Each
+ * round's apply runs beside the next round's chase (double-buffered rotation grids); the
+ * rounds are captured as CUDA graphs and replayed until every matrix has finished. */
 int symeig_qr_batched_f64(symeig_handle h, int64_t count, const int64_t* n, double* d, double* e,
                           double* Q, int32_t max_layers, double tol, int64_t maxiter_factor,
                           int32_t* converged, int64_t* iters);
