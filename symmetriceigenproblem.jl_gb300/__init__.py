@@ -22,7 +22,7 @@ from .api import (  # noqa: F401
     syev,
     sytrd_,
 )
-from ._lib import Handle, SymeigError, default_handle, load as load_library  # noqa: F401
+from ._lib import Handle, SymeigError, default_handle, load as load_library, load_checked  # noqa: F401
 from .build import build, LIB as LIBRARY_PATH  # noqa: F401
 
 try:  # the autograd Functions need torch

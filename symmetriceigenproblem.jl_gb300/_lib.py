@@ -126,6 +126,19 @@ def load(build_if_missing: bool = True):
         return L
 
 
+def load_checked():
+    """The checked build (libsymeig_checked.so, built on first use): the same ABI, with every
+    global access of the wave tiles checked against its pass's extent (see build.build_checked).
+    A separate library instance: its handles are created with its own symeig_create."""
+    path = _build.build_checked()
+    L = ctypes.CDLL(str(path))
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    return L
+
+
 def status_string(status: int) -> str:
     return load().symeig_status_string(status).decode()
 

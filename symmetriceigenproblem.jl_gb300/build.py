@@ -71,5 +71,44 @@ def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | N
     return LIB
 
 
+# The checked build: the translation units that hold the wave tile (the single-matrix and the
+# batched apply) recompiled with -DSYMEIG_DEVICE_CHECKS, linked with the default build's other
+# objects into _build/libsymeig_checked.so.  A debugging aid: every global access of a wave
+# tile is checked against its pass's extent and a failed check is reported as SYMEIG_ERR_DEVICE.
+CHECKED_SOURCES = ["apply.cu", "batched.cu"]
+CHECKED_LIB = OUT / "libsymeig_checked.so"
+
+
+def build_checked(force: bool = False, verbose: bool = False) -> Path:
+    build()
+    if not force and CHECKED_LIB.exists() and CHECKED_LIB.stat().st_mtime >= LIB.stat().st_mtime:
+        return CHECKED_LIB
+    exe = nvcc()
+    cdir = OUT / "checked"
+    cdir.mkdir(exist_ok=True)
+    flags = NVCC_FLAGS + ["-DSYMEIG_DEVICE_CHECKS"]
+
+    def compile_one(src: str):
+        obj = cdir / (Path(src).stem + ".o")
+        r = subprocess.run([exe, *ARCH, *flags, "-c", str(CSRC / src), "-o", str(obj)], capture_output=True, text=True)
+        return src, obj, r
+
+    with ThreadPoolExecutor(max_workers=len(CHECKED_SOURCES)) as ex:
+        results = list(ex.map(compile_one, CHECKED_SOURCES))
+    for src, _, r in results:
+        if verbose or r.returncode != 0:
+            sys.stderr.write(r.stdout + r.stderr)
+        if r.returncode != 0:
+            raise RuntimeError(f"nvcc failed on {src} (checked build)")
+    objs = [str(o) for _, o, _ in results] + [str(OUT / (Path(s).stem + ".o")) for s in SOURCES if s not in CHECKED_SOURCES]
+    tmp = OUT / "libsymeig_checked.so.tmp"
+    r = subprocess.run([exe, *ARCH, "-shared", "-o", str(tmp), *objs], capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError("nvcc link of libsymeig_checked.so failed")
+    os.replace(tmp, CHECKED_LIB)
+    return CHECKED_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose=True))

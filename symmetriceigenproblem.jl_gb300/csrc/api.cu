@@ -174,6 +174,8 @@ int check_device_error(symeig_handle h)
     int derr = 0;
     CK(cudaMemcpy(&derr, h->derr, sizeof(int), cudaMemcpyDeviceToHost));
     h->stats.device_errors = derr;
+    // bit 0: a bounded wait gave up; bit 1: an index check of a checked build failed
+    if (derr & 2) return SYMEIG_ERR_DEVICE;
     return derr ? SYMEIG_ERR_TIMEOUT : SYMEIG_OK;
 }
 

@@ -366,12 +366,15 @@ wave_apply_kernel(T* __restrict__ Q, int64_t ldq, int64_t m, int32_t n_loc,
     __shared__ __align__(128) unsigned char ring[2][Sh::CHUNK];
     __shared__ __align__(8) uint64_t bar[2];
     wave::Staging<Sh> st{ring, bar, 0, 0};
+#ifdef SYMEIG_DEVICE_CHECKS
+    st.check = err;
+#endif
     wave::staging_init(st);
     const int64_t row0 = (int64_t)blockIdx.x * Sh::ROWS;
     T* cta_state = (SEG && state) ? state + (int64_t)blockIdx.x * (wave::segment_state_values<Sh>() * Sh::THREADS) : nullptr;
     if (!wave::wave_tile<T, Sh, SCALED, INT_MUL, SEG>(Q, ldq, m, row0, n_loc, table, n_chunks, nz, st, rs, stall,
                                                       c_begin, c_end, cta_state)) {
-        if (threadIdx.x == 0) atomicExch(err, 1);
+        if (threadIdx.x == 0) atomicOr(err, 1);
     }
 }
 

@@ -204,6 +204,9 @@ batched_wave_kernel(const BatchMat* __restrict__ mats, const Work* __restrict__ 
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int32_t tile_sh;
     wave::Staging<Sh> st{ring, bar, 0, 0};
+#ifdef SYMEIG_DEVICE_CHECKS
+    st.check = err;
+#endif
     wave::staging_init(st);
     const int64_t total = wl->total_tiles[pass][cls];
     for (;;) {
@@ -225,7 +228,7 @@ batched_wave_kernel(const BatchMat* __restrict__ mats, const Work* __restrict__ 
         // FP64: the canonical rotation with its products on the integer pipes (int_mul.cuh)
         if (!wave::wave_tile<T, Sh, false, sizeof(T) == 8>(q, mt.n, mt.n, row0, (int32_t)w.n_loc, tables + toff[lo],
                                                            (int32_t)Sh::chunks(w.n_loc), nz, st)) {
-            if (threadIdx.x == 0) atomicExch(err, 1);
+            if (threadIdx.x == 0) atomicOr(err, 1);
             return;
         }
     }
@@ -451,7 +454,7 @@ int qr_batched_dev(int device, cudaStream_t stream, int64_t count, const int64_t
         }
         int herr = 0;
         CKB(cudaMemcpy(&herr, d_err, sizeof(int), cudaMemcpyDeviceToHost));
-        if (herr) { rc = SYMEIG_ERR_TIMEOUT; goto done; }
+        if (herr) { rc = (herr & 2) ? SYMEIG_ERR_DEVICE : SYMEIG_ERR_TIMEOUT; goto done; }
         CKB(cudaMemcpy(states.data(), d_states, sizeof(ChaseState) * count, cudaMemcpyDeviceToHost));
         for (int64_t i = 0; i < count; ++i) {
             if (converged) converged[i] = states[i].status == CHASE_MAXITER ? 0 : 1;

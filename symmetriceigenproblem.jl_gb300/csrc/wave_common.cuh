@@ -237,7 +237,23 @@ struct Staging {
     unsigned char (*ring)[Sh::CHUNK];
     uint64_t* bar;
     uint32_t uses0, uses1;
+    int* check = nullptr;   // checked builds: the kernel's error word (index_ok)
 };
+
+// Checked builds (-DSYMEIG_DEVICE_CHECKS, build.build_checked): every global access of a wave
+// tile to Q is first checked against the pass's extent (rows [0, m), columns [0, n_loc)); an
+// access outside it is skipped and sets bit 1 (value 2) of the kernel's error word, which the
+// host reports as SYMEIG_ERR_DEVICE.  The default build compiles the checks away.
+#ifdef SYMEIG_DEVICE_CHECKS
+__device__ __forceinline__ bool index_ok(int* check, bool ok)
+{
+    if (!ok && check != nullptr) atomicOr(check, 2);
+    return ok;
+}
+#define WAVE_IDX_OK(st, cond) ::symeig::wave::index_ok((st).check, (cond))
+#else
+#define WAVE_IDX_OK(st, cond) true
+#endif
 
 template <typename Sh>
 __device__ __forceinline__ void staging_init(Staging<Sh>& st)
@@ -359,7 +375,7 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
                 for (int r = 0; r < R; ++r) {
                     const T up = __shfl_up_sync(0xffffffffu, xout[r], RPW);
                     const T xin = (g == 0) ? ahead[r][u % W] : up;
-                    ahead[r][u % W] = *lp[r];
+                    ahead[r][u % W] = WAVE_IDX_OK(st, t0 + W + u < n_loc) ? *lp[r] : T(0);
                     lp[r] += ldq;
                     win[r][u % W] = xin;
                 }
@@ -370,10 +386,11 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     xout[r] = win[r][(u + 1) % W];
+                    const bool in = storer[r] && WAVE_IDX_OK(st, st0 + u >= 0 && st0 + u < n_loc);
                     if constexpr (SCALED) {
-                        if (storer[r]) *sp[r] = xout[r] * dsc;
+                        if (in) *sp[r] = xout[r] * dsc;
                     } else {
-                        if (storer[r]) *sp[r] = xout[r];
+                        if (in) *sp[r] = xout[r];
                     }
                     sp[r] += ldq;
                 }
@@ -389,7 +406,7 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
                     const T up = __shfl_up_sync(0xffffffffu, xout[r], RPW);
                     const T xin = (g == 0) ? ahead[r][u % W] : up;
                     T nxt = T(0);
-                    if (u < ld_cnt) nxt = qrow[r][(int64_t)(t0 + W + u) * ldq];
+                    if (u < ld_cnt && WAVE_IDX_OK(st, t0 + W + u < n_loc)) nxt = qrow[r][(int64_t)(t0 + W + u) * ldq];
                     ahead[r][u % W] = nxt;
                     win[r][u % W] = xin;
                 }
@@ -402,7 +419,9 @@ __device__ __forceinline__ bool wave_tile(T* __restrict__ Q, int64_t ldq, int64_
                     xout[r] = win[r][(u + 1) % W];
                     T xs = xout[r];
                     if constexpr (SCALED) xs = xout[r] * dsc;
-                    st_pred(qrow[r] + (int64_t)(st0 + u) * ldq, xs, storer[r] && u >= st_lo && u < st_hi);
+                    const bool in = storer[r] && u >= st_lo && u < st_hi;
+                    st_pred(qrow[r] + (int64_t)(st0 + u) * ldq, xs,
+                            in && WAVE_IDX_OK(st, st0 + u >= 0 && st0 + u < n_loc));
                 }
             }
         }
