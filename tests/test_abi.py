@@ -32,6 +32,16 @@ def test_library_exports_every_declared_symbol(pkg):
         assert name in pkg._lib.SIGNATURES, f"{name} has no ctypes signature"
 
 
+def test_checked_library_has_the_same_abi(pkg):
+    """The checked build (device index checks in the wave tile) links the same entry points and
+    loads without a GPU; host-side argument checks behave the same."""
+    L = pkg.load_checked()
+    for name in declared_symbols():
+        assert hasattr(L, name), name
+    assert L.symeig_status_string(0) == b"ok"
+    assert L.symeig_apply_givens_f64(None, None, 1, 0, 0, None, 0) == 5
+
+
 def test_status_strings(pkg):
     lib = pkg.load_library()
     assert lib.symeig_status_string(0) == b"ok"
