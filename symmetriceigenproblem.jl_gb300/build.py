@@ -41,73 +41,64 @@ def _stale() -> bool:
     return any(p.stat().st_mtime > t for p in deps if p.exists())
 
 
+def _link(exe: str, objs: list[str], lib: Path):
+    tmp = lib.with_name(lib.name + ".tmp")
+    r = subprocess.run([exe, *ARCH, "-shared", "-o", str(tmp), *objs], capture_output=True, text=True)
+    if r.returncode != 0:
+        sys.stderr.write(r.stdout + r.stderr)
+        raise RuntimeError(f"nvcc link of {lib.name} failed")
+    os.replace(tmp, lib)
+
+
 def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> Path:
+    """Build libsymeig.so and its checked variant (libsymeig_checked.so, build_checked) in one
+    pool of parallel nvcc processes."""
     if not force and not _stale():
         return LIB
     OUT.mkdir(exist_ok=True)
+    (OUT / "checked").mkdir(exist_ok=True)
     exe = nvcc()
     flags = NVCC_FLAGS + (extra_flags or [])
+    jobs = [(src, OUT / (Path(src).stem + ".o"), flags) for src in SOURCES]
+    jobs += [(src, OUT / "checked" / (Path(src).stem + ".o"), flags + ["-DSYMEIG_DEVICE_CHECKS"])
+             for src in CHECKED_SOURCES]
 
-    def compile_one(src: str):
-        obj = OUT / (Path(src).stem + ".o")
-        cmd = [exe, *ARCH, *flags, "-c", str(CSRC / src), "-o", str(obj)]
-        r = subprocess.run(cmd, capture_output=True, text=True)
+    def compile_one(job):
+        src, obj, fl = job
+        r = subprocess.run([exe, *ARCH, *fl, "-c", str(CSRC / src), "-o", str(obj)], capture_output=True, text=True)
         return src, obj, r
 
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        results = list(ex.map(compile_one, SOURCES))
+    with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
+        results = list(ex.map(compile_one, jobs))
     for src, _, r in results:
         if verbose or r.returncode != 0:
             sys.stderr.write(r.stdout + r.stderr)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src}")
-    tmp = OUT / "libsymeig.so.tmp"
-    cmd = [exe, *ARCH, "-shared", "-o", str(tmp), *[str(o) for _, o, _ in results]]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        sys.stderr.write(r.stdout + r.stderr)
-        raise RuntimeError("nvcc link of libsymeig.so failed")
-    os.replace(tmp, LIB)
+    _link(exe, [str(OUT / (Path(s).stem + ".o")) for s in SOURCES], LIB)
+    _link(exe, _checked_objects(), CHECKED_LIB)
     return LIB
 
 
 # The checked build: the translation units that hold the wave tile (the single-matrix and the
-# batched apply) recompiled with -DSYMEIG_DEVICE_CHECKS, linked with the default build's other
+# batched apply) compiled with -DSYMEIG_DEVICE_CHECKS and linked with the default build's other
 # objects into _build/libsymeig_checked.so.  A debugging aid: every global access of a wave
 # tile is checked against its pass's extent and a failed check is reported as SYMEIG_ERR_DEVICE.
 CHECKED_SOURCES = ["apply.cu", "batched.cu"]
 CHECKED_LIB = OUT / "libsymeig_checked.so"
 
 
+def _checked_objects() -> list[str]:
+    return ([str(OUT / "checked" / (Path(s).stem + ".o")) for s in CHECKED_SOURCES] +
+            [str(OUT / (Path(s).stem + ".o")) for s in SOURCES if s not in CHECKED_SOURCES])
+
+
 def build_checked(force: bool = False, verbose: bool = False) -> Path:
-    build()
-    if not force and CHECKED_LIB.exists() and CHECKED_LIB.stat().st_mtime >= LIB.stat().st_mtime:
+    """libsymeig_checked.so (built by build(); rebuilt here if it is missing or older)."""
+    build(force=force, verbose=verbose)
+    if CHECKED_LIB.exists() and CHECKED_LIB.stat().st_mtime >= LIB.stat().st_mtime:
         return CHECKED_LIB
-    exe = nvcc()
-    cdir = OUT / "checked"
-    cdir.mkdir(exist_ok=True)
-    flags = NVCC_FLAGS + ["-DSYMEIG_DEVICE_CHECKS"]
-
-    def compile_one(src: str):
-        obj = cdir / (Path(src).stem + ".o")
-        r = subprocess.run([exe, *ARCH, *flags, "-c", str(CSRC / src), "-o", str(obj)], capture_output=True, text=True)
-        return src, obj, r
-
-    with ThreadPoolExecutor(max_workers=len(CHECKED_SOURCES)) as ex:
-        results = list(ex.map(compile_one, CHECKED_SOURCES))
-    for src, _, r in results:
-        if verbose or r.returncode != 0:
-            sys.stderr.write(r.stdout + r.stderr)
-        if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed on {src} (checked build)")
-    objs = [str(o) for _, o, _ in results] + [str(OUT / (Path(s).stem + ".o")) for s in SOURCES if s not in CHECKED_SOURCES]
-    tmp = OUT / "libsymeig_checked.so.tmp"
-    r = subprocess.run([exe, *ARCH, "-shared", "-o", str(tmp), *objs], capture_output=True, text=True)
-    if r.returncode != 0:
-        sys.stderr.write(r.stdout + r.stderr)
-        raise RuntimeError("nvcc link of libsymeig_checked.so failed")
-    os.replace(tmp, CHECKED_LIB)
-    return CHECKED_LIB
+    return build(force=True, verbose=verbose) and CHECKED_LIB
 
 
 if __name__ == "__main__":
